@@ -1,0 +1,420 @@
+"""fsig_gb300: a GB300-native subgraph-matching engine behind FSIG's interface.
+
+The engine is libfsig.so (hand-written sm_103a CUDA behind the C ABI in
+include/fsig.h); this module binds it with ctypes and mirrors the reference's
+host-side interface:
+
+  UndirectedSurveyPlainReader.read  -> read_graph(path, is_labeled)   (IO/graph_reader.h:27-34)
+  GPUSubgraphMatcher / MMatch / GSI -> MMatch(query, data).match(), GSI(...).match()
+                                       (match/subgraph_match.h:39-81, MMatch.h:75, GSI.h:47)
+  GraphFormatTransformer.transform   -> Engine.build_csr / Engine.build_signature
+
+There is no CPU fallback: when libfsig.so is missing or no sm_103 device is
+present, Engine() raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from pathlib import Path
+from typing import Sequence
+
+import numpy as np
+
+_PKG = Path(__file__).resolve().parent
+_BUILD = _PKG / "_build"
+
+HASH_SEED = 0x46534947B3000001
+MAX_QUERY = 32
+
+OK, EINVAL, ENODEV, ECUDA, EADMISSION, ENOGRAPH, EQUERY, EIO, ETIMEOUT, EOVERFLOW = 0, -1, -2, -3, -4, -5, -6, -7, -8, -9
+ALGO_FSIG, ALGO_GSI, ALGO_FUSED = 1, 2, 3
+ORDER_HEURISTIC, ORDER_LEARNED, ORDER_GIVEN = 0, 1, 2
+QUERY_INDUCED, QUERY_DENSE, QUERY_SPARSE = 0, 1, 2
+
+
+class FsigError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{msg} (status {status})")
+        self.status = status
+
+
+class _Query(C.Structure):
+    _fields_ = [("num_vertices", C.c_uint32), ("num_edges", C.c_uint32), ("labels", C.POINTER(C.c_int32)),
+                ("edges", C.POINTER(C.c_uint32)), ("order", C.POINTER(C.c_uint32))]
+
+
+class _Result(C.Structure):
+    _fields_ = [("count", C.c_uint64), ("hash", C.c_uint64), ("status", C.c_int32), ("num_vertices", C.c_uint32),
+                ("order", C.c_uint32 * MAX_QUERY), ("candidates", C.c_uint32 * MAX_QUERY),
+                ("level_counts", C.c_uint64 * MAX_QUERY), ("ms_filter", C.c_float), ("ms_join", C.c_float)]
+
+
+class _BatchOpts(C.Structure):
+    _fields_ = [("algo", C.c_int), ("order_source", C.c_int), ("refine_iters", C.c_int), ("use_graph", C.c_int),
+                ("chunk", C.c_uint32), ("split_len", C.c_uint32)]
+
+
+_eng = None
+_gen = None
+
+
+def _u32p(a):
+    return a.ctypes.data_as(C.POINTER(C.c_uint32))
+
+
+def _i32p(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+def engine_library() -> C.CDLL:
+    """Loads libfsig.so (built in-tree by fsig_gb300._build); raises if absent."""
+    global _eng
+    if _eng is not None:
+        return _eng
+    path = _BUILD / "libfsig.so"
+    if not path.exists():
+        raise FsigError(ENODEV, f"{path} is missing: build it with fsig_gb300._build.build_all()")
+    L = C.CDLL(str(path))
+    vp = C.c_void_p
+    L.fsig_create.argtypes = [C.c_int, C.c_uint64, C.POINTER(vp)]
+    L.fsig_destroy.argtypes = [vp]
+    L.fsig_last_error.restype = C.c_char_p
+    L.fsig_last_error.argtypes = [vp]
+    L.fsig_status_string.restype = C.c_char_p
+    L.fsig_status_string.argtypes = [C.c_int]
+    L.fsig_load_graph.argtypes = [vp, C.c_uint32, C.POINTER(C.c_int32), C.c_uint64, C.POINTER(C.c_uint32)]
+    L.fsig_load_graph_file.argtypes = [vp, C.c_char_p, C.c_int]
+    L.fsig_graph_info.argtypes = [vp, C.POINTER(C.c_uint32), C.POINTER(C.c_uint64), C.POINTER(C.c_int32),
+                                  C.POINTER(C.c_uint32)]
+    L.fsig_match.argtypes = [vp, C.POINTER(_Query), C.c_int, C.POINTER(_Result)]
+    L.fsig_match_batch.argtypes = [vp, C.c_uint32, C.POINTER(_Query), C.POINTER(_BatchOpts), C.POINTER(_Result)]
+    L.fsig_build_csr.argtypes = [vp, C.c_uint32, C.c_uint64, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
+                                 C.POINTER(C.c_uint32)]
+    L.fsig_build_signature.argtypes = [vp, C.c_uint32, C.POINTER(C.c_int32), C.POINTER(C.c_uint32),
+                                       C.POINTER(C.c_uint32), C.c_int, C.POINTER(C.c_uint32)]
+    L.fsig_filter.argtypes = [vp, C.POINTER(_Query), C.c_int, C.c_int, C.POINTER(C.c_uint8)]
+    for name in ("fsig_create", "fsig_destroy", "fsig_load_graph", "fsig_load_graph_file", "fsig_graph_info",
+                 "fsig_match", "fsig_match_batch", "fsig_build_csr", "fsig_build_signature", "fsig_filter"):
+        getattr(L, name).restype = C.c_int
+    _eng = L
+    return L
+
+
+def gen_library() -> C.CDLL:
+    global _gen
+    if _gen is not None:
+        return _gen
+    path = _BUILD / "libfsig_gen.so"
+    if not path.exists():
+        from . import _build
+        _build.build_gen()
+    L = C.CDLL(str(path))
+    L.fsig_gen_rmat.argtypes = [C.c_uint32, C.c_uint64, C.c_double, C.c_double, C.c_double, C.c_uint64, C.c_int,
+                                C.POINTER(C.c_uint32)]
+    L.fsig_gen_chung_lu.argtypes = [C.c_uint32, C.c_uint64, C.c_double, C.c_uint64, C.c_int, C.POINTER(C.c_uint32)]
+    L.fsig_gen_labels_uniform.argtypes = [C.c_uint32, C.c_uint32, C.c_uint64, C.POINTER(C.c_int32)]
+    L.fsig_gen_labels_zipf.argtypes = [C.c_uint32, C.c_uint32, C.c_double, C.c_uint64, C.POINTER(C.c_int32)]
+    L.fsig_gen_csr.argtypes = [C.c_uint32, C.c_uint64, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
+                               C.POINTER(C.c_uint32), C.POINTER(C.c_uint64)]
+    L.fsig_gen_query.argtypes = [C.c_uint32, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_int32),
+                                 C.c_uint32, C.c_int, C.c_uint64, C.POINTER(C.c_int32), C.POINTER(C.c_uint32),
+                                 C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
+    L.fsig_write_tve.argtypes = [C.c_char_p, C.c_uint32, C.POINTER(C.c_int32), C.c_uint64, C.POINTER(C.c_uint32)]
+    _gen = L
+    return L
+
+
+# ---------------------------------------------------------------------------
+# graphs and queries
+# ---------------------------------------------------------------------------
+@dataclass
+class Graph:
+    """A data graph: labels[V] and an undirected edge list edges[E, 2]."""
+    labels: np.ndarray
+    edges: np.ndarray
+
+    @property
+    def num_vertices(self) -> int:
+        return int(len(self.labels))
+
+    @property
+    def num_edges(self) -> int:
+        return int(len(self.edges))
+
+    def csr(self):
+        """Simple CSR (rows ascending, duplicates and self-loops dropped): (offsets, adj)."""
+        V = self.num_vertices
+        e = np.ascontiguousarray(self.edges, np.uint32).reshape(-1)
+        off = np.zeros(V + 1, np.uint32)
+        adj = np.zeros(max(2 * self.num_edges, 1), np.uint32)
+        n = C.c_uint64()
+        rc = gen_library().fsig_gen_csr(V, self.num_edges, _u32p(e), _u32p(off), _u32p(adj), C.byref(n))
+        if rc:
+            raise FsigError(rc, "csr build failed")
+        return off, adj[: n.value]
+
+    def write_tve(self, path) -> None:
+        lab = np.ascontiguousarray(self.labels, np.int32)
+        e = np.ascontiguousarray(self.edges, np.uint32).reshape(-1)
+        rc = gen_library().fsig_write_tve(str(path).encode(), self.num_vertices, _i32p(lab), self.num_edges, _u32p(e))
+        if rc:
+            raise FsigError(rc, f"cannot write {path}")
+
+
+@dataclass
+class Query:
+    """A query graph: n <= 32 vertices with labels, undirected edges (m, 2)."""
+    labels: np.ndarray
+    edges: np.ndarray
+    order: np.ndarray | None = None
+    source: np.ndarray | None = None  # data vertices it was extracted from (an embedding)
+
+    @property
+    def num_vertices(self) -> int:
+        return int(len(self.labels))
+
+    def write_tve(self, path) -> None:
+        Graph(np.asarray(self.labels, np.int32), np.asarray(self.edges, np.uint32).reshape(-1, 2)).write_tve(path)
+
+
+@dataclass
+class Result:
+    count: int
+    hash: int
+    status: int
+    order: list
+    candidates: list
+    level_counts: list
+    ms_filter: float = 0.0
+    ms_join: float = 0.0
+
+
+def read_graph(path, is_labeled: bool = True) -> Graph:
+    """Host reader with the reference's semantics (IO/graph_reader.cc:12-55),
+    returning the edge list (duplicates kept) and labels."""
+    labels, edges = [], []
+    vmax = -1
+    lab = {}
+    text = Path(path).read_text()
+    toks = text.split()
+    if not toks or toks[0] != "t":
+        raise FsigError(EIO, f"{path}: not a t/v/e file")
+    i = 3
+    while i < len(toks):
+        t = toks[i]
+        if t == "v":
+            vid, l = int(toks[i + 1]), int(toks[i + 2])
+            lab[vid] = l if is_labeled else 0
+            vmax = max(vmax, vid)
+            i += 4
+        elif t == "e":
+            edges.append((int(toks[i + 1]), int(toks[i + 2])))
+            i += 3
+        else:
+            i += 1
+    if text and text[-1].isspace() and toks and edges and toks[-3] == "e":
+        edges.append(edges[-1])  # the reference's loop applies its last record twice
+    labels = np.full(vmax + 1, -1, np.int32)
+    for k, v in lab.items():
+        labels[k] = v
+    return Graph(labels, np.asarray(edges, np.uint32).reshape(-1, 2))
+
+
+def read_query(path, is_labeled: bool = True) -> Query:
+    g = read_graph(path, is_labeled)
+    return Query(g.labels, g.edges)
+
+
+# ---------------------------------------------------------------------------
+# generators (seeded synthetic workloads)
+# ---------------------------------------------------------------------------
+def gen_rmat(V: int, E: int, a=0.57, b=0.19, c=0.19, seed=1, labels=None, threads=0) -> Graph:
+    e = np.zeros(2 * E, np.uint32)
+    rc = gen_library().fsig_gen_rmat(V, E, a, b, c, seed, threads, _u32p(e))
+    if rc:
+        raise FsigError(rc, "R-MAT generation failed")
+    lab = np.zeros(V, np.int32) if labels is None else labels
+    return Graph(lab, e.reshape(-1, 2))
+
+
+def gen_chung_lu(V: int, E: int, gamma: float, seed=2, labels=None, threads=0) -> Graph:
+    e = np.zeros(2 * E, np.uint32)
+    rc = gen_library().fsig_gen_chung_lu(V, E, gamma, seed, threads, _u32p(e))
+    if rc:
+        raise FsigError(rc, "Chung-Lu generation failed")
+    lab = np.zeros(V, np.int32) if labels is None else labels
+    return Graph(lab, e.reshape(-1, 2))
+
+
+def gen_labels(V: int, L: int, dist: str = "uniform", seed=1, s: float = 1.0) -> np.ndarray:
+    lab = np.zeros(V, np.int32)
+    if dist == "uniform":
+        rc = gen_library().fsig_gen_labels_uniform(V, L, seed, _i32p(lab))
+    else:
+        rc = gen_library().fsig_gen_labels_zipf(V, L, s, seed, _i32p(lab))
+    if rc:
+        raise FsigError(rc, "label generation failed")
+    return lab
+
+
+def gen_query(g: Graph, n: int, mode: int = QUERY_INDUCED, seed: int = 1, csr=None) -> Query:
+    off, adj = csr if csr is not None else g.csr()
+    lab = np.ascontiguousarray(g.labels, np.int32)
+    ql = np.zeros(n, np.int32)
+    qe = np.zeros(n * (n - 1), np.uint32)
+    m = C.c_uint32()
+    src = np.zeros(n, np.uint32)
+    adj = np.ascontiguousarray(adj if len(adj) else np.zeros(1, np.uint32), np.uint32)
+    rc = gen_library().fsig_gen_query(g.num_vertices, _u32p(off), _u32p(adj), _i32p(lab), n, mode, seed, _i32p(ql),
+                                      _u32p(qe), C.byref(m), _u32p(src))
+    if rc:
+        raise FsigError(rc, f"query extraction gave up (n={n}, mode={mode}, seed={seed})")
+    return Query(ql, qe[: 2 * m.value].reshape(-1, 2).copy(), source=src)
+
+
+# ---------------------------------------------------------------------------
+# engine
+# ---------------------------------------------------------------------------
+def _as_cquery(q: Query, keep: list) -> _Query:
+    lab = np.ascontiguousarray(q.labels, np.int32)
+    e = np.ascontiguousarray(np.asarray(q.edges, np.uint32).reshape(-1))
+    keep += [lab, e]
+    cq = _Query(len(lab), len(e) // 2, _i32p(lab), _u32p(e) if e.size else None, None)
+    if q.order is not None:
+        o = np.ascontiguousarray(q.order, np.uint32)
+        keep.append(o)
+        cq.order = _u32p(o)
+    return cq
+
+
+def _result(r: _Result) -> Result:
+    n = r.num_vertices
+    return Result(int(r.count), int(r.hash), int(r.status), list(r.order[:n]), list(r.candidates[:n]),
+                  [int(x) for x in r.level_counts[:n]], float(r.ms_filter), float(r.ms_join))
+
+
+class Engine:
+    """One device arena on one GPU; replaces init_GPU + MemoryManager."""
+
+    def __init__(self, device: int = 0, arena_bytes: int = 0):
+        self._L = engine_library()
+        h = C.c_void_p()
+        rc = self._L.fsig_create(device, arena_bytes, C.byref(h))
+        if rc:
+            raise FsigError(rc, "fsig_create: " + self._L.fsig_last_error(None).decode())
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.fsig_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc: int, what: str):
+        if rc:
+            raise FsigError(rc, f"{what}: {self._L.fsig_last_error(self._h).decode()}")
+
+    # data graph
+    def load_graph(self, g: Graph) -> None:
+        lab = np.ascontiguousarray(g.labels, np.int32)
+        e = np.ascontiguousarray(g.edges, np.uint32).reshape(-1)
+        if e.size == 0:
+            e = np.zeros(2, np.uint32)
+        self._check(self._L.fsig_load_graph(self._h, len(lab), _i32p(lab), g.num_edges, _u32p(e)), "load_graph")
+
+    def load_graph_file(self, path, is_labeled: bool = True) -> None:
+        self._check(self._L.fsig_load_graph_file(self._h, str(path).encode(), 1 if is_labeled else 0),
+                    "load_graph_file")
+
+    def graph_info(self) -> dict:
+        V, nadj, L, md = C.c_uint32(), C.c_uint64(), C.c_int32(), C.c_uint32()
+        self._check(self._L.fsig_graph_info(self._h, C.byref(V), C.byref(nadj), C.byref(L), C.byref(md)),
+                    "graph_info")
+        return dict(V=V.value, adj=nadj.value, L=L.value, max_degree=md.value)
+
+    # matching
+    def match(self, q: Query, algo: int = ALGO_FSIG) -> Result:
+        keep = []
+        cq = _as_cquery(q, keep)
+        r = _Result()
+        self._check(self._L.fsig_match(self._h, C.byref(cq), algo, C.byref(r)), "match")
+        return _result(r)
+
+    def match_batch(self, qs: Sequence[Query], algo: int = ALGO_FUSED, order_source: int = ORDER_HEURISTIC,
+                    refine_iters: int = -1, chunk: int = 0, use_graph: bool = False) -> list:
+        keep = []
+        arr = (_Query * max(len(qs), 1))()
+        for i, q in enumerate(qs):
+            arr[i] = _as_cquery(q, keep)
+        res = (_Result * max(len(qs), 1))()
+        opts = _BatchOpts(algo, order_source, refine_iters, 1 if use_graph else 0, chunk, 0)
+        self._check(self._L.fsig_match_batch(self._h, len(qs), arr, C.byref(opts), res), "match_batch")
+        return [_result(res[i]) for i in range(len(qs))]
+
+    # transforms and filter probe
+    def build_csr(self, V: int, edges: np.ndarray):
+        e = np.ascontiguousarray(edges, np.uint32).reshape(-1)
+        E = e.size // 2
+        off = np.zeros(V + 1, np.uint32)
+        adj = np.zeros(max(2 * E, 1), np.uint32)
+        if e.size == 0:
+            e = np.zeros(2, np.uint32)
+        self._check(self._L.fsig_build_csr(self._h, V, E, _u32p(e), _u32p(off), _u32p(adj)), "build_csr")
+        return off, adj[: 2 * E]
+
+    def build_signature(self, labels, offsets, adj, column_oriented: bool = False) -> np.ndarray:
+        lab = np.ascontiguousarray(labels, np.int32)
+        off = np.ascontiguousarray(offsets, np.uint32)
+        a = np.ascontiguousarray(adj, np.uint32)
+        if a.size == 0:
+            a = np.zeros(1, np.uint32)
+        out = np.zeros(16 * len(lab), np.uint32)
+        self._check(self._L.fsig_build_signature(self._h, len(lab), _i32p(lab), _u32p(off), _u32p(a),
+                                                 1 if column_oriented else 0, _u32p(out)), "build_signature")
+        return out
+
+    def filter(self, q: Query, algo: int = ALGO_GSI, refine_iters: int = -1) -> np.ndarray:
+        keep = []
+        cq = _as_cquery(q, keep)
+        V = self.graph_info()["V"]
+        out = np.zeros(q.num_vertices * V, np.uint8)
+        self._check(self._L.fsig_filter(self._h, C.byref(cq), algo, refine_iters,
+                                        out.ctypes.data_as(C.POINTER(C.c_uint8))), "filter")
+        return out.reshape(q.num_vertices, V)
+
+
+class GPUSubgraphMatcher:
+    """Mirror of GPUSubgraphMatcher(Graph* query, Graph* data) with match()
+    (match/subgraph_match.h:39-81).  The data graph is loaded into the engine
+    on construction; match() returns the Result instead of printing it."""
+    algo = ALGO_FUSED
+
+    def __init__(self, query_graph: Query, data_graph: Graph, dev_id: int = 0, engine: Engine | None = None):
+        self.query_graph = query_graph
+        self.data_graph = data_graph
+        self.engine = engine or Engine(dev_id)
+        if engine is None:
+            self.engine.load_graph(data_graph)
+
+    def match(self) -> Result:
+        return self.engine.match(self.query_graph, self.algo)
+
+
+class MMatch(GPUSubgraphMatcher):
+    algo = ALGO_FSIG
+
+
+class GSI(GPUSubgraphMatcher):
+    algo = ALGO_GSI

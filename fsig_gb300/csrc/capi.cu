@@ -1,0 +1,281 @@
+// C ABI of libfsig (include/fsig.h).
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "engine.h"
+#include "match.h"
+#include "reader.h"
+
+namespace fsig {
+
+namespace {
+thread_local std::string t_err;
+}
+
+int fail_cuda(cudaError_t e, const char* what, const char* file, int line) {
+  t_err = std::string(cudaGetErrorString(e)) + " in " + what + " (" + file + ":" + std::to_string(line) + ")";
+  return FSIG_ECUDA;
+}
+int fail(int status, const std::string& msg) {
+  t_err = msg;
+  return status;
+}
+const std::string& thread_error() { return t_err; }
+void clear_thread_error() { t_err.clear(); }
+
+}  // namespace fsig
+
+using fsig::Engine;
+
+struct fsig_engine {
+  Engine e;
+};
+
+namespace {
+
+int finish(fsig_engine* h, int rc) {
+  if (rc != FSIG_OK && h) h->e.last_error = fsig::thread_error();
+  return rc;
+}
+
+int select(fsig_engine* h) {
+  if (!h) return FSIG_EINVAL;
+  cudaError_t err = cudaSetDevice(h->e.device);
+  if (err != cudaSuccess) return fsig::fail_cuda(err, "cudaSetDevice", __FILE__, __LINE__);
+  fsig::clear_thread_error();
+  return FSIG_OK;
+}
+
+void fill_result(const fsig::HostQuery& hq, const fsig::BatchOutput& o, uint32_t qi, uint32_t g0, fsig_result* r) {
+  r->count = o.res[qi].count;
+  r->hash = o.res[qi].hash;
+  r->status = FSIG_OK;
+  r->num_vertices = hq.n;
+  for (uint32_t i = 0; i < FSIG_MAX_QUERY; i++) {
+    r->order[i] = i < hq.n ? o.orders[size_t(qi) * FSIG_MAX_QUERY + i] : 0;
+    r->candidates[i] = i < hq.n ? o.counts[g0 + i] : 0;
+    r->level_counts[i] = i < hq.n ? o.res[qi].levels[i] : 0;
+  }
+  r->ms_filter = o.ms_filter;
+  r->ms_join = o.ms_join;
+}
+
+void algo_options(int algo, int refine_iters, fsig::BatchOptions& o) {
+  if (algo == FSIG_ALGO_FSIG) {
+    o.filter_mode = fsig::kFilterDegree;
+    o.refine_iters = refine_iters >= 0 ? refine_iters : 3;
+    o.order_mode = fsig::kOrderMMatch;
+  } else if (algo == FSIG_ALGO_GSI) {
+    o.filter_mode = fsig::kFilterSignature;
+    o.refine_iters = refine_iters >= 0 ? refine_iters : 0;
+    o.order_mode = fsig::kOrderGSI;
+  } else {
+    o.filter_mode = fsig::kFilterDegree | fsig::kFilterSignature;
+    o.refine_iters = refine_iters >= 0 ? refine_iters : 2;
+    o.order_mode = fsig::kOrderGSI;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* fsig_status_string(int s) {
+  switch (s) {
+    case FSIG_OK: return "ok";
+    case FSIG_EINVAL: return "invalid argument";
+    case FSIG_ENODEV: return "no usable CUDA device";
+    case FSIG_ECUDA: return "CUDA error";
+    case FSIG_EADMISSION: return "request does not fit the device arena";
+    case FSIG_ENOGRAPH: return "no data graph loaded";
+    case FSIG_EQUERY: return "invalid query";
+    case FSIG_EIO: return "file error";
+    case FSIG_ETIMEOUT: return "device wait timed out";
+    case FSIG_EOVERFLOW: return "device work queue overflow";
+    default: return "unknown status";
+  }
+}
+
+const char* fsig_last_error(const fsig_engine* h) {
+  if (!h) return fsig::thread_error().c_str();
+  return h->e.last_error.c_str();
+}
+
+int fsig_create(int device, uint64_t arena_bytes, fsig_engine** out) {
+  if (!out) return FSIG_EINVAL;
+  *out = nullptr;
+  fsig::clear_thread_error();
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= device || device < 0) {
+    fsig::fail(FSIG_ENODEV, "no CUDA device with this index");
+    return FSIG_ENODEV;
+  }
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return FSIG_ENODEV;
+  if (prop.major != 10 || prop.minor != 3) {
+    fsig::fail(FSIG_ENODEV, std::string("libfsig is built for sm_103 only; device is ") + prop.name);
+    return FSIG_ENODEV;
+  }
+  auto* h = new (std::nothrow) fsig_engine();
+  if (!h) return FSIG_EINVAL;
+  Engine& e = h->e;
+  e.device = device;
+  e.num_sms = prop.multiProcessorCount;
+  int rc = FSIG_OK;
+  auto bail = [&](int code) {
+    h->e.last_error = fsig::thread_error();
+    if (e.arena.base) cudaFree(e.arena.base);
+    if (e.stream) cudaStreamDestroy(e.stream);
+    delete h;
+    return code;
+  };
+  cudaError_t err = cudaSetDevice(device);
+  if (err != cudaSuccess) return bail(fsig::fail_cuda(err, "cudaSetDevice", __FILE__, __LINE__));
+  err = cudaStreamCreateWithFlags(&e.stream, cudaStreamNonBlocking);
+  if (err != cudaSuccess) return bail(fsig::fail_cuda(err, "cudaStreamCreate", __FILE__, __LINE__));
+  for (auto& ev : e.ev) {
+    err = cudaEventCreate(&ev);
+    if (err != cudaSuccess) return bail(fsig::fail_cuda(err, "cudaEventCreate", __FILE__, __LINE__));
+  }
+  uint64_t bytes = arena_bytes ? arena_bytes : uint64_t(prop.totalGlobalMem) / 4;
+  err = cudaMalloc(&e.arena.base, bytes);
+  if (err != cudaSuccess) return bail(fsig::fail(FSIG_EADMISSION, "cannot reserve the device arena"));
+  e.arena.cap = bytes;
+  (void)rc;
+  *out = h;
+  return FSIG_OK;
+}
+
+int fsig_destroy(fsig_engine* h) {
+  if (!h) return FSIG_EINVAL;
+  cudaSetDevice(h->e.device);
+  if (h->e.stream) cudaStreamSynchronize(h->e.stream);
+  for (auto& ev : h->e.ev)
+    if (ev) cudaEventDestroy(ev);
+  if (h->e.arena.base) cudaFree(h->e.arena.base);
+  if (h->e.pinned) cudaFreeHost(h->e.pinned);
+  if (h->e.stream) cudaStreamDestroy(h->e.stream);
+  delete h;
+  return FSIG_OK;
+}
+
+int fsig_load_graph(fsig_engine* h, uint32_t V, const int32_t* labels, uint64_t E, const uint32_t* edges) {
+  int rc = select(h);
+  if (rc) return finish(h, rc);
+  if (!labels || (E && !edges)) return finish(h, fsig::fail(FSIG_EINVAL, "graph arrays missing"));
+  return finish(h, fsig::build_device_graph(h->e, V, labels, E, edges));
+}
+
+int fsig_load_graph_file(fsig_engine* h, const char* path, int is_labeled) {
+  int rc = select(h);
+  if (rc) return finish(h, rc);
+  if (!path) return finish(h, fsig::fail(FSIG_EINVAL, "no path"));
+  fsig::TveGraph g;
+  std::string err;
+  if (fsig::read_tve(path, is_labeled, g, err) != 0) return finish(h, fsig::fail(FSIG_EIO, err));
+  for (uint32_t v = 0; v < g.num_vertices; v++)
+    if (g.labels[v] < 0) return finish(h, fsig::fail(FSIG_EIO, "vertex " + std::to_string(v) + " has no v record"));
+  for (uint32_t x : g.edges)
+    if (x >= g.num_vertices) return finish(h, fsig::fail(FSIG_EIO, "edge endpoint without a v record"));
+  return finish(h, fsig::build_device_graph(h->e, g.num_vertices, g.labels.data(), g.edges.size() / 2,
+                                            g.edges.data()));
+}
+
+int fsig_graph_info(const fsig_engine* h, uint32_t* V, uint64_t* nadj, int32_t* L, uint32_t* maxdeg) {
+  if (!h) return FSIG_EINVAL;
+  if (!h->e.has_graph) return FSIG_ENOGRAPH;
+  if (V) *V = h->e.g.V;
+  if (nadj) *nadj = h->e.g.nadj;
+  if (L) *L = h->e.g.L;
+  if (maxdeg) *maxdeg = h->e.g.max_deg;
+  return FSIG_OK;
+}
+
+int fsig_match(fsig_engine* h, const fsig_query* q, int algo, fsig_result* out) {
+  int rc = select(h);
+  if (rc) return finish(h, rc);
+  if (!q || !out) return finish(h, fsig::fail(FSIG_EINVAL, "null argument"));
+  if (algo != FSIG_ALGO_FSIG && algo != FSIG_ALGO_GSI && algo != FSIG_ALGO_FUSED)
+    return finish(h, fsig::fail(FSIG_EINVAL, "unknown algorithm"));
+  std::memset(out, 0, sizeof(*out));
+  std::vector<fsig::HostQuery> qs(1);
+  rc = fsig::prepare_query(*q, h->e.has_graph ? h->e.g.L : 0, qs[0]);
+  if (rc) { out->status = rc; return finish(h, rc); }
+  fsig::BatchOptions o;
+  algo_options(algo, -1, o);
+  if (!qs[0].has_given) o.host_order = algo == FSIG_ALGO_FSIG ? fsig::mmatch_order_host : fsig::gsi_order_host;
+  else o.order_mode = fsig::kOrderGiven;
+  fsig::BatchOutput bo;
+  rc = fsig::run_batch(h->e, qs, o, bo);
+  if (rc) { out->status = rc; return finish(h, rc); }
+  fill_result(qs[0], bo, 0, 0, out);
+  return FSIG_OK;
+}
+
+int fsig_match_batch(fsig_engine* h, uint32_t nq, const fsig_query* qs, const fsig_batch_opts* opts,
+                     fsig_result* out) {
+  int rc = select(h);
+  if (rc) return finish(h, rc);
+  if ((nq && (!qs || !out))) return finish(h, fsig::fail(FSIG_EINVAL, "null argument"));
+  fsig_batch_opts def{FSIG_ALGO_FUSED, FSIG_ORDER_HEURISTIC, -1, 0, 0, 0};
+  const fsig_batch_opts& bo = opts ? *opts : def;
+  if (bo.algo != FSIG_ALGO_FSIG && bo.algo != FSIG_ALGO_GSI && bo.algo != FSIG_ALGO_FUSED)
+    return finish(h, fsig::fail(FSIG_EINVAL, "unknown algorithm"));
+  std::vector<fsig::HostQuery> hq;
+  std::vector<uint32_t> idx;
+  hq.reserve(nq);
+  for (uint32_t i = 0; i < nq; i++) {
+    std::memset(&out[i], 0, sizeof(fsig_result));
+    fsig::HostQuery x;
+    int r = fsig::prepare_query(qs[i], h->e.has_graph ? h->e.g.L : 0, x);
+    if (r) { out[i].status = r; continue; }
+    if (bo.order_source == FSIG_ORDER_GIVEN && !x.has_given) { out[i].status = FSIG_EQUERY; continue; }
+    hq.push_back(std::move(x));
+    idx.push_back(i);
+  }
+  fsig::BatchOptions o;
+  algo_options(bo.algo, bo.refine_iters, o);
+  if (bo.order_source == FSIG_ORDER_GIVEN) o.order_mode = fsig::kOrderGiven;
+  else if (bo.order_source == FSIG_ORDER_LEARNED) return finish(h, fsig::fail(FSIG_EINVAL, "no order network loaded"));
+  if (bo.chunk) o.chunk = bo.chunk;
+  fsig::BatchOutput out_b;
+  rc = fsig::run_batch(h->e, hq, o, out_b);
+  if (rc) return finish(h, rc);
+  uint32_t g0 = 0;
+  for (size_t k = 0; k < hq.size(); k++) {
+    fill_result(hq[k], out_b, uint32_t(k), g0, &out[idx[k]]);
+    g0 += hq[k].n;
+  }
+  return FSIG_OK;
+}
+
+int fsig_build_csr(fsig_engine* h, uint32_t V, uint64_t E, const uint32_t* edges, uint32_t* offsets, uint32_t* adj) {
+  int rc = select(h);
+  if (rc) return finish(h, rc);
+  if (!offsets || (E && (!edges || !adj))) return finish(h, fsig::fail(FSIG_EINVAL, "null argument"));
+  return finish(h, fsig::build_reference_csr(h->e, V, E, edges, offsets, adj));
+}
+
+int fsig_build_signature(fsig_engine* h, uint32_t V, const int32_t* labels, const uint32_t* offsets,
+                         const uint32_t* adj, int column_oriented, uint32_t* signature) {
+  int rc = select(h);
+  if (rc) return finish(h, rc);
+  if (!labels || !offsets || !signature) return finish(h, fsig::fail(FSIG_EINVAL, "null argument"));
+  return finish(h, fsig::build_reference_signature(h->e, V, labels, offsets, adj, column_oriented, signature));
+}
+
+int fsig_filter(fsig_engine* h, const fsig_query* q, int algo, int refine_iters, uint8_t* flags) {
+  int rc = select(h);
+  if (rc) return finish(h, rc);
+  if (!q || !flags) return finish(h, fsig::fail(FSIG_EINVAL, "null argument"));
+  fsig::HostQuery hq;
+  rc = fsig::prepare_query(*q, h->e.has_graph ? h->e.g.L : 0, hq);
+  if (rc) return finish(h, rc);
+  fsig::BatchOptions o;
+  algo_options(algo, refine_iters, o);
+  return finish(h, fsig::run_filter_probe(h->e, hq, o.filter_mode, o.refine_iters, flags));
+}
+
+}  // extern "C"

@@ -1,0 +1,58 @@
+// Engine state shared by the libfsig translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+
+namespace fsig {
+
+// The resident data graph, renumbered so that every label class occupies a
+// contiguous id range: new ids are sorted by (label, caller id).  In this id
+// space a row of the adjacency sorted by id is also sorted by neighbour
+// label, so the neighbours of v with label l are one contiguous segment
+// [lseg[v*(L+1)+l], lseg[v*(L+1)+l+1]) -- the label-partitioned layout that
+// replaces the reference's hashed PCSR units.
+struct DeviceGraph {
+  uint32_t V = 0;
+  int32_t L = 0;
+  uint64_t nadj = 0;
+  uint32_t max_deg = 0;
+  int32_t* label = nullptr;        // [V]   label of each new id
+  uint32_t* old_of_new = nullptr;  // [V]
+  uint32_t* new_of_old = nullptr;  // [V]
+  uint32_t* base = nullptr;        // [L+1] first new id of each label class
+  uint32_t* off = nullptr;         // [V+1]
+  uint32_t* adj = nullptr;         // [nadj] new ids, rows ascending, no duplicates
+  uint32_t* lseg = nullptr;        // [V*(L+1)]
+  uint4* sig = nullptr;            // [V*4] 64-byte signature per vertex
+  std::vector<uint32_t> h_base;    // host copy of base
+  uint64_t arena_mark = 0;         // arena top after the graph store
+};
+
+struct Engine {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  Arena arena;
+  DeviceGraph g;
+  bool has_graph = false;
+  std::string last_error;
+  // pinned host staging for batches
+  void* pinned = nullptr;
+  uint64_t pinned_bytes = 0;
+  // timing events
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+};
+
+// graph_store.cu
+int build_device_graph(Engine& e, uint32_t V, const int32_t* labels, uint64_t E, const uint32_t* edges);
+int build_reference_csr(Engine& e, uint32_t V, uint64_t E, const uint32_t* edges, uint32_t* offsets,
+                        uint32_t* adj);
+int build_reference_signature(Engine& e, uint32_t V, const int32_t* labels, const uint32_t* offsets,
+                              const uint32_t* adj, int column_oriented, uint32_t* sig);
+
+}  // namespace fsig

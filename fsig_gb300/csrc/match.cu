@@ -1,0 +1,881 @@
+// Batch matching: candidate filter, neighbour-support refinement, candidate
+// counts, device-side ordering, root compaction and the DFS enumerator.
+//
+// Reference counterparts:
+//   filter_kernel / scatter_kernel            match/GSI_kernels.cuh:8-36
+//   initialise_kernel / scatter_kernel        match/MMatch_kernels.cuh:6-26
+//   count_neighbors_kernel + check_re_kernel  match/MMatch_kernels.cuh:28-117, 190-214
+//   GSI::generate_join_order                  match/GSI.cu:105-149
+//   MMatch::generate_join_order               match/MMatch.cu:1575-1641
+//   GSI join kernels                          match/GSI_kernels.cuh:95-560
+//   MMatch join kernels                       match/MMatch_kernels.cuh:374-820
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "match.h"
+#include "scan.cuh"
+
+namespace fsig {
+
+struct GraphView {
+  uint32_t V;
+  int32_t L;
+  const int32_t* __restrict__ label;
+  const uint32_t* __restrict__ off;
+  const uint32_t* __restrict__ adj;
+  const uint32_t* __restrict__ lseg;
+  const uint4* __restrict__ sig;
+  const uint32_t* __restrict__ old_of_new;
+};
+
+namespace {
+
+constexpr uint32_t kFull = 0xffffffffu;
+constexpr int kChunk = 32;  // driver elements examined per refill (one per lane)
+
+GraphView view_of(const DeviceGraph& g) {
+  return GraphView{g.V, g.L, g.label, g.off, g.adj, g.lseg, g.sig, g.old_of_new};
+}
+
+// ---------------------------------------------------------------------------
+// Filter: one warp per aligned group of 32 (renumbered) data vertices.  The
+// group's vertices carry one or a few labels (ids are label-sorted); for each
+// query vertex of such a label the warp evaluates the tests lane-parallel and
+// writes one bitmap word with a ballot.  Every bitmap word is written exactly
+// once, so no clearing pass is needed.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) filter_kernel(GraphView g, const QVert* __restrict__ qv,
+                                                     const uint32_t* __restrict__ lab_gidx,
+                                                     const uint32_t* __restrict__ lab_begin, uint32_t mode,
+                                                     uint32_t* __restrict__ pool) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t nwt = (gridDim.x * blockDim.x) >> 5;
+  const uint32_t ngroups = (g.V + 31) >> 5;
+  for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < ngroups; w += nwt) {
+    const uint32_t v = (w << 5) + lane;
+    const bool live = v < g.V;
+    const int32_t l = live ? g.label[v] : -1;
+    const uint32_t deg = live ? g.off[v + 1] - g.off[v] : 0;
+    uint4 s0 = make_uint4(0, 0, 0, 0), s1 = s0, s2 = s0, s3 = s0;
+    if ((mode & kFilterSignature) && live) {
+      const uint4* p = g.sig + uint64_t(v) * 4;
+      s0 = p[0]; s1 = p[1]; s2 = p[2]; s3 = p[3];
+    }
+    const int32_t lfirst = __shfl_sync(kFull, l, 0);
+    const uint32_t last_lane = min(31u, g.V - 1 - (w << 5));
+    const int32_t llast = __shfl_sync(kFull, l, last_lane);
+    for (int32_t lab = lfirst; lab <= llast; lab++) {
+      const uint32_t b = lab_begin[lab], e = lab_begin[lab + 1];
+      for (uint32_t i = b; i < e; i++) {
+        const QVert* q = qv + lab_gidx[i];
+        bool p = l == lab;
+        if (mode & kFilterDegree) p = p && deg >= q->deg;
+        if (mode & kFilterSignature) {
+          const uint4* qs = reinterpret_cast<const uint4*>(q->sig);
+          uint4 a = qs[0], bb = qs[1], c = qs[2], d = qs[3];
+          // word 0 (the label) is covered by l == lab
+          bool sub = ((a.y & s0.y) == a.y) & ((a.z & s0.z) == a.z) & ((a.w & s0.w) == a.w) &
+                     ((bb.x & s1.x) == bb.x) & ((bb.y & s1.y) == bb.y) & ((bb.z & s1.z) == bb.z) &
+                     ((bb.w & s1.w) == bb.w) & ((c.x & s2.x) == c.x) & ((c.y & s2.y) == c.y) &
+                     ((c.z & s2.z) == c.z) & ((c.w & s2.w) == c.w) & ((d.x & s3.x) == d.x) &
+                     ((d.y & s3.y) == d.y) & ((d.z & s3.z) == d.z) & ((d.w & s3.w) == d.w);
+          p = p && sub;
+        }
+        const uint32_t word = __ballot_sync(kFull, p);
+        if (lane == 0 && q->words) pool[q->bmoff + (w - (q->bmbase >> 5))] = word;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// One Jacobi step of neighbour-support refinement: v stays in C(u) only if for
+// every query neighbour w of u some neighbour of v (in the label-l(w) segment)
+// is in C(w) as read from src.  Warps take runs of bitmap words.
+// ---------------------------------------------------------------------------
+constexpr uint32_t kRefineRun = 8;
+
+__global__ void __launch_bounds__(256) refine_kernel(GraphView g, const QVert* __restrict__ qv, uint32_t G,
+                                                     const uint64_t* __restrict__ gword, uint64_t total_words,
+                                                     const uint32_t* __restrict__ src, uint32_t* __restrict__ dst) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint64_t nwt = (uint64_t(gridDim.x) * blockDim.x) >> 5;
+  const uint64_t W1 = uint64_t(g.L) + 1;
+  for (uint64_t run = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; run * kRefineRun < total_words;
+       run += nwt) {
+    uint64_t W = run * kRefineRun;
+    const uint64_t Wend = min(W + kRefineRun, total_words);
+    // query vertex owning word W: last g with gword[g] <= W
+    uint32_t lo = 0, hi = G;
+    while (hi - lo > 1) {
+      uint32_t mid = (lo + hi) >> 1;
+      if (gword[mid] <= W) lo = mid; else hi = mid;
+    }
+    uint32_t gi = lo;
+    for (; W < Wend; W++) {
+      while (gword[gi + 1] <= W) gi++;
+      const QVert* q = qv + gi;
+      const uint32_t word = src[W];
+      if (word == 0 || q->adj == 0) {
+        if (lane == 0) dst[W] = word;
+        continue;
+      }
+      const uint32_t v = q->bmbase + uint32_t((W - q->bmoff) << 5) + lane;
+      bool alive = (word >> lane) & 1u;
+      uint32_t m = q->adj;
+      const uint32_t gbase = gi - q->u;
+      while (m) {
+        const uint32_t wv = __ffs(m) - 1;
+        m &= m - 1;
+        const QVert* qw = qv + gbase + wv;
+        if (alive) {
+          if (qw->words == 0) {
+            alive = false;
+          } else {
+            const uint32_t* s = g.lseg + uint64_t(v) * W1 + qw->label;
+            uint32_t k = s[0];
+            const uint32_t e = s[1];
+            bool found = false;
+            for (; k < e; k++) {
+              const uint32_t bit = g.adj[k] - qw->bmbase;
+              if ((src[qw->bmoff + (bit >> 5)] >> (bit & 31)) & 1u) { found = true; break; }
+            }
+            alive = found;
+          }
+        }
+      }
+      const uint32_t nw = __ballot_sync(kFull, alive);
+      if (lane == 0) dst[W] = nw;
+    }
+  }
+}
+
+// Candidates per query vertex (popcount of its bitmap).
+__global__ void __launch_bounds__(256) popcount_kernel(const QVert* __restrict__ qv, uint32_t G,
+                                                       const uint32_t* __restrict__ pool, uint32_t* counts) {
+  __shared__ uint32_t red[8];
+  for (uint32_t gi = blockIdx.x; gi < G; gi += gridDim.x) {
+    const QVert* q = qv + gi;
+    uint32_t c = 0;
+    for (uint32_t i = threadIdx.x; i < q->words; i += blockDim.x) c += __popc(pool[q->bmoff + i]);
+    c = warp_sum(c);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      uint32_t t = 0;
+      for (int i = 0; i < int(blockDim.x >> 5); i++) t += red[i];
+      counts[gi] = t;
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Ordering: one warp per query, lane u = query vertex u.  Greedy frontier
+// argmin of a score with ties to the lowest vertex id.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t warp_argmin(float s, uint32_t id) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    float s2 = __shfl_xor_sync(kFull, s, o);
+    uint32_t i2 = __shfl_xor_sync(kFull, id, o);
+    if (s2 < s || (s2 == s && i2 < id)) { s = s2; id = i2; }
+  }
+  return id;
+}
+
+__global__ void order_kernel(const QVert* __restrict__ qv, const uint32_t* __restrict__ qoff, uint32_t Q,
+                             const uint32_t* __restrict__ counts, uint32_t mode, const float* __restrict__ scores,
+                             const uint32_t* __restrict__ given, Plan* plans, uint32_t* root_count,
+                             uint32_t* orders_out) {
+  const uint32_t lane = threadIdx.x & 31;
+  for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < Q; q += (gridDim.x * blockDim.x) >> 5) {
+    const uint32_t g0 = qoff[q], n = qoff[q + 1] - g0;
+    const bool live = lane < n;
+    const uint32_t all = n == 32 ? kFull : ((1u << n) - 1);
+    const QVert* me = qv + g0 + (live ? lane : 0);
+    const uint32_t cnt = live ? counts[g0 + lane] : 0;
+    const uint32_t adj = live ? me->adj : 0;
+    const int32_t lab = live ? me->label : -1;
+    const uint32_t deg = live ? me->deg : 0;
+    const bool ok = n > 0 && __ballot_sync(kFull, live && cnt == 0) == 0;
+
+    float score = float(cnt);
+    uint32_t root_only = kFull;  // position 0 restricted to this vertex when != kFull
+    if (mode == kOrderMMatch) {
+      // 2-core by peeling vertices of degree <= 1 (match/MMatch.cu:543-607)
+      uint32_t alive = all;
+      for (int it = 0; it < 32; it++) {
+        const bool in = live && ((alive >> lane) & 1u) && __popc(adj & alive) <= 1;
+        const uint32_t peel = __ballot_sync(kFull, in);
+        if (!peel) break;
+        alive &= ~peel;
+      }
+      const uint32_t type = ((alive >> lane) & 1u) ? 2u : (deg == 1 ? 0u : 1u);
+      float maxc = 0.f, maxf = 0.f;
+      float myc = (live && type == 2) ? float(cnt) : 0.f, myf = (live && type == 1) ? float(cnt) : 0.f;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        myc = fmaxf(myc, __shfl_xor_sync(kFull, myc, o));
+        myf = fmaxf(myf, __shfl_xor_sync(kFull, myf, o));
+      }
+      maxc = myc;
+      maxf = myf;
+      if (type == 0) score = (float(cnt) + maxf) + maxc;
+      else if (type == 1) score = float(cnt) + maxc;
+      if (alive == 0) {
+        // no core: root = forest vertex of least BFS weight (MMatch.cu:270-315)
+        uint32_t visited = 1u << lane, frontier = visited, weight = 0;
+        for (uint32_t level = 0; level < n; level++) {
+          uint32_t next = 0;
+          for (uint32_t j = 0; j < n; j++) {
+            uint32_t mj = __shfl_sync(kFull, adj, j);
+            if ((frontier >> j) & 1u) next |= mj;
+          }
+          next &= ~visited & all;
+          weight += __popc(next) * (level + 1);
+          visited |= next;
+          frontier = next;
+        }
+        const bool cand = live && type == 1;
+        const uint32_t any = __ballot_sync(kFull, cand);
+        if (any) root_only = warp_argmin(cand ? float(weight) : INFINITY, cand ? lane : 0xffffu);
+      }
+    } else if (mode == kOrderScores) {
+      score = live ? scores[g0 + lane] : 0.f;
+    }
+
+    uint32_t myord = 0, placed = 0;
+    if (mode == kOrderGiven) {
+      myord = live ? given[g0 + lane] : 0;
+    } else {
+      for (uint32_t i = 0; i < n; i++) {
+        bool elig = live && !((placed >> lane) & 1u);
+        if (i == 0) elig = elig && (root_only == kFull || lane == root_only);
+        else elig = elig && (adj & placed) != 0;
+        const uint32_t u = warp_argmin(elig ? score : INFINITY, elig ? lane : 0xffffu);
+        if (u >= n) break;  // cannot happen for connected queries
+        placed |= 1u << u;
+        if (lane == i) myord = u;
+        if (mode == kOrderGSI && live && ((adj >> u) & 1u)) score = float(double(score) * 0.9);
+      }
+    }
+    // Plan for position i = lane.
+    const uint32_t u = myord;
+    const uint32_t adj_u = __shfl_sync(kFull, adj, u);
+    const int32_t lab_u = __shfl_sync(kFull, lab, u);
+    uint32_t bwd = 0, same = 0;
+    for (uint32_t j = 0; j < n; j++) {
+      const uint32_t uj = __shfl_sync(kFull, myord, j);
+      const int32_t lj = __shfl_sync(kFull, lab, uj);
+      if (j < lane) {
+        if ((adj_u >> uj) & 1u) bwd |= 1u << j;
+        if (lj == lab_u) same |= 1u << j;
+      }
+    }
+    Plan* p = plans + q;
+    if (live) {
+      const QVert* qu = qv + g0 + u;
+      p->qv[lane] = u;
+      p->lab[lane] = lab_u;
+      p->bwd[lane] = bwd;
+      p->same[lane] = same;
+      p->bmbase[lane] = qu->bmbase;
+      p->bmoff[lane] = qu->bmoff;
+      orders_out[uint64_t(q) * kMaxQ + lane] = u;
+    }
+    if (lane == 0) {
+      p->n = n;
+      p->ok = ok ? 1u : 0u;
+      p->g0 = g0;
+      root_count[q] = ok ? counts[g0 + u] : 0u;
+    }
+  }
+}
+
+// Roots of each query in ascending vertex order (block scan of word popcounts).
+__global__ void __launch_bounds__(256) roots_kernel(const QVert* __restrict__ qv, const Plan* __restrict__ plans,
+                                                    uint32_t Q, const uint32_t* __restrict__ root_off,
+                                                    const uint32_t* __restrict__ pool, uint32_t* roots) {
+  __shared__ uint32_t sw[33];
+  for (uint32_t q = blockIdx.x; q < Q; q += gridDim.x) {
+    const Plan* p = plans + q;
+    if (!p->ok) continue;
+    const QVert* r = qv + p->g0 + p->qv[0];
+    uint32_t outp = root_off[q];
+    for (uint32_t b = 0; b < r->words; b += blockDim.x) {
+      const uint32_t i = b + threadIdx.x;
+      const uint32_t word = i < r->words ? pool[r->bmoff + i] : 0u;
+      uint32_t total;
+      uint32_t ex = block_exclusive_scan<uint32_t>(__popc(word), sw, total);
+      uint32_t wbits = word;
+      uint32_t k = outp + ex;
+      while (wbits) {
+        const uint32_t bit = __ffs(wbits) - 1;
+        wbits &= wbits - 1;
+        roots[k++] = r->bmbase + (i << 5) + bit;
+      }
+      outp += total;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Enumeration: a persistent grid; each warp repeatedly takes `chunk` root
+// tasks from a global counter and runs a depth-first extension of each root.
+//
+// Level state lives in registers distributed over lanes: lane j holds, for
+// depth j, the mapped vertex f_j, the partial hash S_j, the driver cursor
+// (dpos_j, dend_j, drv_j) and the candidate buffer cursor (cnt_j, it_j).  The
+// candidate buffers (32 per depth) and the plan live in shared memory.
+//
+// Candidates at depth i are the driver list (the shortest label-l(i) segment
+// among the backward neighbours' rows), examined 32 at a time, one per lane:
+// injectivity against same-label earlier positions, the candidate bitmap of
+// position i, then a binary search in every other backward segment.
+// ---------------------------------------------------------------------------
+struct WarpSmem {
+  Plan plan;
+  uint32_t cand[kMaxQ][kChunk];
+};
+
+__device__ __forceinline__ bool contains(const uint32_t* __restrict__ a, uint32_t lo, uint32_t hi, uint32_t x,
+                                         unsigned long long& bytes) {
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    const uint32_t y = __ldg(a + mid);
+    bytes += 4;
+    if (y < x) lo = mid + 1;
+    else if (y > x) hi = mid;
+    else return true;
+  }
+  return false;
+}
+
+__global__ void __launch_bounds__(256) enumerate_kernel(GraphView g, const Plan* __restrict__ plans,
+                                                        const uint32_t* __restrict__ pool,
+                                                        const uint32_t* __restrict__ roots,
+                                                        const uint32_t* __restrict__ root_off, uint32_t Q,
+                                                        uint32_t chunk, uint32_t* task_next, QueryResult* res,
+                                                        unsigned long long* algo_bytes, unsigned long long seed) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  WarpSmem& ws = reinterpret_cast<WarpSmem*>(smem_raw)[threadIdx.x >> 5];
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t T = root_off[Q];
+  const uint64_t W1 = uint64_t(g.L) + 1;
+
+  // lane-distributed level state
+  uint32_t f = 0, dpos = 0, dend = 0, drv = 0, cnt = 0, it = 0;
+  unsigned long long S = 0, lc = 0;
+  unsigned long long my_count = 0, my_hash = 0, bytes = 0;
+  uint32_t cur_q = kInvalid;
+
+  auto flush = [&](uint32_t q) {
+    if (q == kInvalid) return;
+    unsigned long long c = warp_sum(my_count), h = warp_sum(my_hash);
+    if (lane == 0) {
+      atomicAdd(&res[q].count, c);
+      atomicAdd(&res[q].hash, h);
+    }
+    if (lane < ws.plan.n && lc) atomicAdd(&res[q].levels[lane], lc);
+    my_count = my_hash = 0;
+    lc = 0;
+  };
+
+  // Computes the driver of depth `lv` from the mapped vertices of its
+  // backward neighbours; stores it in lane lv's registers.
+  auto enter = [&](uint32_t lv) {
+    const uint32_t bw = ws.plan.bwd[lv];
+    const int32_t lab = ws.plan.lab[lv];
+    uint32_t lo = 0, hi = 0, len = kInvalid;
+    if ((bw >> lane) & 1u) {
+      const uint32_t* s = g.lseg + uint64_t(f) * W1 + lab;
+      lo = s[0];
+      hi = s[1];
+      len = hi - lo;
+      bytes += 8;
+    }
+    const bool empty = __ballot_sync(kFull, len == 0) != 0;
+    const uint32_t j = warp_argmin(float(len), len == kInvalid ? 0xffffu : lane);
+    const uint32_t dlo = __shfl_sync(kFull, lo, j & 31), dhi = __shfl_sync(kFull, hi, j & 31);
+    if (lane == lv) {
+      dpos = dlo;
+      dend = empty ? dlo : dhi;
+      drv = j;
+      cnt = 0;
+      it = 0;
+    }
+  };
+
+  // Examines the next 32 driver entries of depth lv; returns the candidate
+  // predicate and the candidate (one per lane).
+  auto examine = [&](uint32_t lv, uint32_t& x) -> bool {
+    const uint32_t dp = __shfl_sync(kFull, dpos, lv), de = __shfl_sync(kFull, dend, lv);
+    const uint32_t dv = __shfl_sync(kFull, drv, lv);
+    const int32_t lab = ws.plan.lab[lv];
+    uint32_t bw = ws.plan.bwd[lv] & ~(1u << dv);
+    uint32_t my_lo = 0, my_hi = 0;
+    if ((bw >> lane) & 1u) {
+      const uint32_t* s = g.lseg + uint64_t(f) * W1 + lab;
+      my_lo = s[0];
+      my_hi = s[1];
+      bytes += 8;
+    }
+    const uint32_t k = dp + lane;
+    bool pred = k < de;
+    x = pred ? __ldg(g.adj + k) : 0u;
+    if (pred) bytes += 4;
+    uint32_t sm = ws.plan.same[lv];
+    while (sm) {
+      const uint32_t j = __ffs(sm) - 1;
+      sm &= sm - 1;
+      const uint32_t fj = __shfl_sync(kFull, f, j);
+      pred = pred && x != fj;
+    }
+    if (pred) {
+      const uint32_t bit = x - ws.plan.bmbase[lv];
+      pred = (__ldg(pool + ws.plan.bmoff[lv] + (bit >> 5)) >> (bit & 31)) & 1u;
+      bytes += 4;
+    }
+    while (bw) {
+      const uint32_t j = __ffs(bw) - 1;
+      bw &= bw - 1;
+      const uint32_t lo = __shfl_sync(kFull, my_lo, j), hi = __shfl_sync(kFull, my_hi, j);
+      if (pred) pred = contains(g.adj, lo, hi, x, bytes);
+    }
+    if (lane == lv) dpos = dp + kChunk;
+    return pred;
+  };
+
+  for (;;) {
+    uint32_t t0 = 0;
+    if (lane == 0) t0 = atomicAdd(task_next, chunk);
+    t0 = __shfl_sync(kFull, t0, 0);
+    if (t0 >= T) break;
+    const uint32_t t1 = min(t0 + chunk, T);
+    for (uint32_t t = t0; t < t1; t++) {
+      if (cur_q == kInvalid || t < root_off[cur_q] || t >= root_off[cur_q + 1]) {
+        uint32_t lo = 0, hi = Q;  // last q with root_off[q] <= t
+        while (hi - lo > 1) {
+          const uint32_t mid = (lo + hi) >> 1;
+          if (root_off[mid] <= t) lo = mid; else hi = mid;
+        }
+        while (lo + 1 < Q && root_off[lo + 1] <= t) lo++;
+        flush(cur_q);
+        __syncwarp();
+        const uint32_t* src = reinterpret_cast<const uint32_t*>(plans + lo);
+        uint32_t* dstp = reinterpret_cast<uint32_t*>(&ws.plan);
+        for (uint32_t i = lane; i < sizeof(Plan) / 4; i += 32) dstp[i] = src[i];
+        __syncwarp();
+        cur_q = lo;
+      }
+      const uint32_t n = ws.plan.n;
+      const uint32_t r = roots[t];
+      const unsigned long long S0 = fmix64((uint64_t(ws.plan.qv[0]) << 32) | g.old_of_new[r]);
+      if (lane == 0) {
+        f = r;
+        S = S0;
+        lc += 1;
+      }
+      if (n == 1) {
+        if (lane == 0) {
+          my_count += 1;
+          my_hash += fmix64(seed + S0);
+        }
+        continue;
+      }
+      uint32_t lv = 1;
+      enter(1);
+      while (true) {
+        if (lv == n - 1) {
+          // leaf depth: count and hash every surviving candidate
+          const unsigned long long Sp = __shfl_sync(kFull, S, lv - 1);
+          const uint64_t tb = uint64_t(ws.plan.qv[lv]) << 32;
+          while (__shfl_sync(kFull, dpos, lv) < __shfl_sync(kFull, dend, lv)) {
+            uint32_t x;
+            const bool p = examine(lv, x);
+            const uint32_t m = __ballot_sync(kFull, p);
+            if (p) {
+              my_count += 1;
+              my_hash += fmix64(seed + Sp + fmix64(tb | __ldg(g.old_of_new + x)));
+              bytes += 4;
+            }
+            if (lane == lv) lc += __popc(m);
+          }
+          lv--;
+          if (lv == 0) break;
+          continue;
+        }
+        const uint32_t i = __shfl_sync(kFull, it, lv), c = __shfl_sync(kFull, cnt, lv);
+        if (i < c) {
+          const uint32_t x = ws.cand[lv][i];
+          const unsigned long long Sp = __shfl_sync(kFull, S, lv - 1);
+          if (lane == lv) {
+            it = i + 1;
+            f = x;
+            S = Sp + fmix64((uint64_t(ws.plan.qv[lv]) << 32) | __ldg(g.old_of_new + x));
+            bytes += 4;
+          }
+          lv++;
+          enter(lv);
+          continue;
+        }
+        if (__shfl_sync(kFull, dpos, lv) < __shfl_sync(kFull, dend, lv)) {
+          uint32_t x;
+          const bool p = examine(lv, x);
+          const uint32_t m = __ballot_sync(kFull, p);
+          if (p) ws.cand[lv][__popc(m & lanemask_lt())] = x;
+          __syncwarp();
+          if (lane == lv) {
+            cnt = __popc(m);
+            it = 0;
+            lc += __popc(m);
+          }
+          continue;
+        }
+        lv--;
+        if (lv == 0) break;
+      }
+    }
+  }
+  flush(cur_q);
+  bytes = warp_sum(bytes);
+  if (lane == 0) atomicAdd(algo_bytes, bytes);
+}
+
+inline unsigned grid_cap(uint64_t n, int threads, int sms, int per_sm) {
+  uint64_t b = (n + threads - 1) / threads;
+  uint64_t cap = uint64_t(sms) * per_sm;
+  if (b > cap) b = cap;
+  return unsigned(b ? b : 1);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+int prepare_query(const fsig_query& q, int32_t num_labels, HostQuery& h) {
+  (void)num_labels;
+  h = HostQuery();
+  if (q.num_vertices == 0 || q.num_vertices > uint32_t(kMaxQ)) return fail(FSIG_EQUERY, "query size must be 1..32");
+  if (!q.labels || (q.num_edges && !q.edges)) return fail(FSIG_EINVAL, "query arrays missing");
+  const uint32_t n = q.num_vertices;
+  h.n = n;
+  h.nbr.assign(n, std::vector<uint32_t>());
+  for (uint32_t u = 0; u < n; u++) {
+    h.label[u] = q.labels[u];
+    h.adj[u] = 0;
+  }
+  for (uint32_t e = 0; e < q.num_edges; e++) {
+    const uint32_t a = q.edges[2 * e], b = q.edges[2 * e + 1];
+    if (a >= n || b >= n) return fail(FSIG_EQUERY, "query edge endpoint out of range");
+    h.nbr[a].push_back(b);
+    h.nbr[b].push_back(a);
+    if (a == b) continue;
+    h.adj[a] |= 1u << b;
+    h.adj[b] |= 1u << a;
+  }
+  for (uint32_t u = 0; u < n; u++) h.deg[u] = uint32_t(__builtin_popcount(h.adj[u]));
+  // connectivity
+  uint32_t seen = 1u, frontier = 1u;
+  while (frontier) {
+    uint32_t next = 0;
+    for (uint32_t u = 0; u < n; u++)
+      if ((frontier >> u) & 1u) next |= h.adj[u];
+    frontier = next & ~seen;
+    seen |= next;
+  }
+  const uint32_t all = n == 32 ? 0xffffffffu : ((1u << n) - 1);
+  if ((seen & all) != all) return fail(FSIG_EQUERY, "query graph is disconnected");
+  // signature of every query vertex (graph_format_transformer.cc:217-262)
+  for (uint32_t u = 0; u < n; u++) {
+    std::memset(h.sig[u], 0, sizeof(h.sig[u]));
+    h.sig[u][0] = uint32_t(h.label[u]);
+    for (uint32_t w = 0; w < n; w++) {
+      if (!((h.adj[u] >> w) & 1u)) continue;
+      uint32_t word, sh;
+      sig_slot(h.label[w], word, sh);
+      const uint32_t cur = (h.sig[u][word] >> sh) & 3u;
+      h.sig[u][word] |= (cur == 0 ? 1u : 3u) << sh;
+    }
+  }
+  if (q.order) {
+    uint32_t seenv = 0;
+    for (uint32_t i = 0; i < n; i++) {
+      if (q.order[i] >= n || ((seenv >> q.order[i]) & 1u)) return fail(FSIG_EQUERY, "order is not a permutation");
+      seenv |= 1u << q.order[i];
+      h.given[i] = q.order[i];
+    }
+    // every position after the first needs a placed neighbour
+    uint32_t placed = 1u << h.given[0];
+    for (uint32_t i = 1; i < n; i++) {
+      if (!(h.adj[h.given[i]] & placed)) return fail(FSIG_EQUERY, "order is not connected");
+      placed |= 1u << h.given[i];
+    }
+    h.has_given = true;
+  }
+  return FSIG_OK;
+}
+
+namespace {
+struct BatchLayout {
+  uint32_t Q = 0, G = 0;
+  uint64_t words = 0;
+  uint64_t root_cap = 0;
+  std::vector<QVert> qv;
+  std::vector<uint32_t> qoff, lab_gidx, lab_begin;
+  std::vector<uint64_t> gword;
+};
+
+void layout_batch(const DeviceGraph& g, const std::vector<HostQuery>& qs, BatchLayout& b) {
+  b.Q = uint32_t(qs.size());
+  b.qoff.assign(size_t(b.Q) + 1, 0);
+  for (uint32_t q = 0; q < b.Q; q++) b.qoff[q + 1] = b.qoff[q] + qs[q].n;
+  b.G = b.qoff[b.Q];
+  b.qv.assign(b.G, QVert());
+  b.gword.assign(size_t(b.G) + 1, 0);
+  std::vector<std::vector<uint32_t>> by_label(size_t(g.L));
+  uint64_t w = 0, rc = 0;
+  for (uint32_t q = 0; q < b.Q; q++) {
+    const HostQuery& h = qs[q];
+    uint64_t qmax = 0;
+    for (uint32_t u = 0; u < h.n; u++) {
+      const uint32_t gi = b.qoff[q] + u;
+      QVert& x = b.qv[gi];
+      std::memset(&x, 0, sizeof(x));
+      x.label = h.label[u];
+      x.deg = h.deg[u];
+      x.adj = h.adj[u];
+      x.q = q;
+      x.u = u;
+      std::memcpy(x.sig, h.sig[u], sizeof(x.sig));
+      const int32_t l = h.label[u];
+      uint32_t lo = 0, hi = 0;
+      if (l >= 0 && l < g.L) { lo = g.h_base[l]; hi = g.h_base[l + 1]; }
+      if (hi > lo) {
+        x.bmbase = lo & ~31u;
+        x.words = ((hi + 31) >> 5) - (lo >> 5);
+        by_label[size_t(l)].push_back(gi);
+        qmax = std::max<uint64_t>(qmax, hi - lo);
+      } else {
+        x.bmbase = 0;
+        x.words = 0;
+      }
+      x.bmoff = w;
+      b.gword[gi] = w;
+      w += x.words;
+    }
+    rc += qmax;
+  }
+  b.gword[b.G] = w;
+  b.words = w;
+  b.root_cap = rc;
+  b.lab_begin.assign(size_t(g.L) + 1, 0);
+  b.lab_gidx.clear();
+  for (int32_t l = 0; l < g.L; l++) {
+    b.lab_begin[size_t(l)] = uint32_t(b.lab_gidx.size());
+    b.lab_gidx.insert(b.lab_gidx.end(), by_label[size_t(l)].begin(), by_label[size_t(l)].end());
+  }
+  b.lab_begin[size_t(g.L)] = uint32_t(b.lab_gidx.size());
+}
+
+template <class T>
+T* upload(Engine& e, const std::vector<T>& v, int& rc) {
+  T* d = e.arena.take<T>(std::max<size_t>(v.size(), 1));
+  if (!d) { rc = fail(FSIG_EADMISSION, "batch does not fit the device arena"); return nullptr; }
+  if (!v.empty()) {
+    cudaError_t err = cudaMemcpyAsync(d, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, e.stream);
+    if (err != cudaSuccess) { rc = fail_cuda(err, "cudaMemcpyAsync", __FILE__, __LINE__); return nullptr; }
+  }
+  return d;
+}
+
+// Filter + refine + popcount on the device.  Returns the final pool.
+int filter_stage(Engine& e, const BatchLayout& b, uint32_t mode, int refine_iters, QVert* d_qv, uint64_t* d_gword,
+                 uint32_t* d_lab_gidx, uint32_t* d_lab_begin, uint32_t*& pool, uint32_t* d_counts) {
+  const DeviceGraph& g = e.g;
+  cudaStream_t s = e.stream;
+  uint32_t* p0 = e.arena.take<uint32_t>(std::max<uint64_t>(b.words, 1));
+  uint32_t* p1 = refine_iters > 0 ? e.arena.take<uint32_t>(std::max<uint64_t>(b.words, 1)) : nullptr;
+  if (!p0 || (refine_iters > 0 && !p1)) return fail(FSIG_EADMISSION, "candidate bitmaps do not fit the arena");
+  const GraphView gv = view_of(g);
+  filter_kernel<<<grid_cap(uint64_t(g.V), 256, e.num_sms, 16), 256, 0, s>>>(gv, d_qv, d_lab_gidx, d_lab_begin, mode,
+                                                                           p0);
+  FSIG_CUDA_TRY(cudaGetLastError());
+  uint32_t* cur = p0;
+  uint32_t* nxt = p1;
+  for (int it = 0; it < refine_iters && b.words; it++) {
+    const uint64_t runs = (b.words + kRefineRun - 1) / kRefineRun;
+    refine_kernel<<<grid_cap(runs * 32, 256, e.num_sms, 16), 256, 0, s>>>(gv, d_qv, b.G, d_gword, b.words, cur, nxt);
+    FSIG_CUDA_TRY(cudaGetLastError());
+    std::swap(cur, nxt);
+  }
+  if (b.G) {
+    popcount_kernel<<<std::min<uint32_t>(b.G, e.num_sms * 8), 256, 0, s>>>(d_qv, b.G, cur, d_counts);
+    FSIG_CUDA_TRY(cudaGetLastError());
+  }
+  pool = cur;
+  return FSIG_OK;
+}
+}  // namespace
+
+int run_batch(Engine& e, const std::vector<HostQuery>& qs, const BatchOptions& opt, BatchOutput& out) {
+  if (!e.has_graph) return fail(FSIG_ENOGRAPH, "no data graph loaded");
+  const DeviceGraph& g = e.g;
+  cudaStream_t s = e.stream;
+  BatchLayout b;
+  layout_batch(g, qs, b);
+  const uint32_t Q = b.Q;
+  out.res.assign(Q, QueryResult());
+  out.counts.assign(b.G, 0);
+  out.orders.assign(size_t(Q) * kMaxQ, 0);
+  out.ok.assign(Q, 0);
+  if (Q == 0) return FSIG_OK;
+  if (b.root_cap > 0xffffffffull) return fail(FSIG_EADMISSION, "batch has more than 2^32 root candidates");
+  e.arena.release(g.arena_mark);
+  int rc = FSIG_OK;
+  QVert* d_qv = upload(e, b.qv, rc);
+  if (rc) return rc;
+  uint32_t* d_qoff = upload(e, b.qoff, rc);
+  if (rc) return rc;
+  uint32_t* d_lab_gidx = upload(e, b.lab_gidx, rc);
+  if (rc) return rc;
+  uint32_t* d_lab_begin = upload(e, b.lab_begin, rc);
+  if (rc) return rc;
+  uint64_t* d_gword = upload(e, b.gword, rc);
+  if (rc) return rc;
+  std::vector<uint32_t> given(b.G, 0);
+  std::vector<float> scores(b.G, 0.f);
+  for (uint32_t q = 0; q < Q; q++)
+    for (uint32_t i = 0; i < qs[q].n; i++) {
+      given[b.qoff[q] + i] = qs[q].has_given ? qs[q].given[i] : i;
+      if (opt.scores) scores[b.qoff[q] + i] = opt.scores[b.qoff[q] + i];
+    }
+  uint32_t* d_given = upload(e, given, rc);
+  if (rc) return rc;
+  float* d_scores = upload(e, scores, rc);
+  if (rc) return rc;
+  uint32_t* d_counts = e.arena.take<uint32_t>(std::max<uint32_t>(b.G, 1));
+  Plan* d_plans = e.arena.take<Plan>(Q);
+  uint32_t* d_rootcnt = e.arena.take<uint32_t>(uint64_t(Q) + 1);
+  uint32_t* d_rootoff = e.arena.take<uint32_t>(uint64_t(Q) + 1);
+  uint32_t* d_orders = e.arena.take<uint32_t>(uint64_t(Q) * kMaxQ);
+  QueryResult* d_res = e.arena.take<QueryResult>(Q);
+  unsigned long long* d_misc = e.arena.take<unsigned long long>(4);  // [0] task_next, [1] algo bytes
+  if (!d_counts || !d_plans || !d_rootcnt || !d_rootoff || !d_orders || !d_res || !d_misc)
+    return fail(FSIG_EADMISSION, "batch does not fit the device arena");
+
+  FSIG_CUDA_TRY(cudaEventRecord(e.ev[0], s));
+  uint32_t* pool = nullptr;
+  rc = filter_stage(e, b, opt.filter_mode, opt.refine_iters, d_qv, d_gword, d_lab_gidx, d_lab_begin, pool, d_counts);
+  if (rc) return rc;
+  FSIG_CUDA_TRY(cudaEventRecord(e.ev[1], s));
+
+  uint32_t order_mode = opt.order_mode;
+  if (opt.host_order) {
+    // Reference-exact orders are computed on the host from the counts.
+    FSIG_CUDA_TRY(cudaMemcpyAsync(out.counts.data(), d_counts, sizeof(uint32_t) * b.G, cudaMemcpyDeviceToHost, s));
+    FSIG_CUDA_TRY(cudaStreamSynchronize(s));
+    for (uint32_t q = 0; q < Q; q++) {
+      bool any_zero = false;
+      for (uint32_t u = 0; u < qs[q].n; u++) any_zero |= out.counts[b.qoff[q] + u] == 0;
+      if (qs[q].has_given) continue;
+      if (any_zero) {  // nothing to enumerate; any connected order will do
+        for (uint32_t i = 0; i < qs[q].n; i++) given[b.qoff[q] + i] = i;
+        uint32_t placed = 1u;
+        for (uint32_t i = 1; i < qs[q].n; i++)
+          for (uint32_t u = 0; u < qs[q].n; u++)
+            if (!((placed >> u) & 1u) && (qs[q].adj[u] & placed)) { given[b.qoff[q] + i] = u; placed |= 1u << u; break; }
+        continue;
+      }
+      opt.host_order(qs[q], out.counts.data() + b.qoff[q], given.data() + b.qoff[q]);
+    }
+    FSIG_CUDA_TRY(cudaMemcpyAsync(d_given, given.data(), sizeof(uint32_t) * b.G, cudaMemcpyHostToDevice, s));
+    order_mode = kOrderGiven;
+  }
+  uint32_t* d_roots = e.arena.take<uint32_t>(std::max<uint64_t>(b.root_cap, 1));
+  if (!d_roots) return fail(FSIG_EADMISSION, "root list does not fit the device arena");
+  FSIG_CUDA_TRY(cudaMemsetAsync(d_rootcnt, 0, sizeof(uint32_t) * (uint64_t(Q) + 1), s));
+  order_kernel<<<(Q + 7) / 8, 256, 0, s>>>(d_qv, d_qoff, Q, d_counts, order_mode, d_scores, d_given, d_plans,
+                                           d_rootcnt, d_orders);
+  FSIG_CUDA_TRY(cudaGetLastError());
+  rc = device_exclusive_scan<uint32_t>(e.arena, d_rootcnt, d_rootoff, uint64_t(Q) + 1, nullptr, s);
+  if (rc) return rc;
+  roots_kernel<<<std::min<uint32_t>(Q, e.num_sms * 8), 256, 0, s>>>(d_qv, d_plans, Q, d_rootoff, pool, d_roots);
+  FSIG_CUDA_TRY(cudaGetLastError());
+  FSIG_CUDA_TRY(cudaMemsetAsync(d_res, 0, sizeof(QueryResult) * Q, s));
+  FSIG_CUDA_TRY(cudaMemsetAsync(d_misc, 0, sizeof(unsigned long long) * 4, s));
+  const uint32_t wpb = std::max<uint32_t>(1, std::min<uint32_t>(opt.warps_per_block, 8));
+  const size_t smem = sizeof(WarpSmem) * wpb;
+  FSIG_CUDA_TRY(cudaFuncSetAttribute(enumerate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+  int per_sm = 0;
+  FSIG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, enumerate_kernel, int(wpb * 32), smem));
+  per_sm = std::max(per_sm, 1);
+  enumerate_kernel<<<e.num_sms * per_sm, wpb * 32, smem, s>>>(
+      view_of(g), d_plans, pool, d_roots, d_rootoff, Q, std::max<uint32_t>(opt.chunk, 1),
+      reinterpret_cast<uint32_t*>(d_misc), d_res, d_misc + 1, FSIG_HASH_SEED);
+  FSIG_CUDA_TRY(cudaGetLastError());
+  FSIG_CUDA_TRY(cudaEventRecord(e.ev[2], s));
+
+  FSIG_CUDA_TRY(cudaMemcpyAsync(out.res.data(), d_res, sizeof(QueryResult) * Q, cudaMemcpyDeviceToHost, s));
+  FSIG_CUDA_TRY(cudaMemcpyAsync(out.counts.data(), d_counts, sizeof(uint32_t) * b.G, cudaMemcpyDeviceToHost, s));
+  FSIG_CUDA_TRY(cudaMemcpyAsync(out.orders.data(), d_orders, sizeof(uint32_t) * Q * kMaxQ, cudaMemcpyDeviceToHost, s));
+  FSIG_CUDA_TRY(cudaMemcpyAsync(&out.algo_bytes, d_misc + 1, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+  std::vector<Plan> hp(Q);
+  FSIG_CUDA_TRY(cudaMemcpyAsync(hp.data(), d_plans, sizeof(Plan) * Q, cudaMemcpyDeviceToHost, s));
+  FSIG_CUDA_TRY(cudaStreamSynchronize(s));
+  for (uint32_t q = 0; q < Q; q++) out.ok[q] = hp[q].ok;
+  FSIG_CUDA_TRY(cudaEventElapsedTime(&out.ms_filter, e.ev[0], e.ev[1]));
+  FSIG_CUDA_TRY(cudaEventElapsedTime(&out.ms_join, e.ev[1], e.ev[2]));
+  e.arena.release(g.arena_mark);
+  return FSIG_OK;
+}
+
+int run_filter_probe(Engine& e, const HostQuery& q, uint32_t filter_mode, int refine_iters, uint8_t* flags) {
+  if (!e.has_graph) return fail(FSIG_ENOGRAPH, "no data graph loaded");
+  const DeviceGraph& g = e.g;
+  std::vector<HostQuery> qs(1, q);
+  BatchLayout b;
+  layout_batch(g, qs, b);
+  e.arena.release(g.arena_mark);
+  int rc = FSIG_OK;
+  QVert* d_qv = upload(e, b.qv, rc);
+  if (rc) return rc;
+  uint32_t* d_lab_gidx = upload(e, b.lab_gidx, rc);
+  if (rc) return rc;
+  uint32_t* d_lab_begin = upload(e, b.lab_begin, rc);
+  if (rc) return rc;
+  uint64_t* d_gword = upload(e, b.gword, rc);
+  if (rc) return rc;
+  uint32_t* d_counts = e.arena.take<uint32_t>(std::max<uint32_t>(b.G, 1));
+  if (!d_counts) return fail(FSIG_EADMISSION, "arena");
+  uint32_t* pool = nullptr;
+  rc = filter_stage(e, b, filter_mode, refine_iters, d_qv, d_gword, d_lab_gidx, d_lab_begin, pool, d_counts);
+  if (rc) return rc;
+  std::vector<uint32_t> hpool(b.words);
+  std::vector<uint32_t> old_of_new(g.V);
+  if (b.words)
+    FSIG_CUDA_TRY(cudaMemcpyAsync(hpool.data(), pool, sizeof(uint32_t) * b.words, cudaMemcpyDeviceToHost, e.stream));
+  FSIG_CUDA_TRY(cudaMemcpyAsync(old_of_new.data(), g.old_of_new, sizeof(uint32_t) * g.V, cudaMemcpyDeviceToHost,
+                                e.stream));
+  FSIG_CUDA_TRY(cudaStreamSynchronize(e.stream));
+  e.arena.release(g.arena_mark);
+  std::memset(flags, 0, size_t(q.n) * g.V);
+  for (uint32_t u = 0; u < q.n; u++) {
+    const QVert& x = b.qv[u];
+    for (uint32_t w = 0; w < x.words; w++) {
+      uint32_t word = hpool[x.bmoff + w];
+      while (word) {
+        const uint32_t bit = uint32_t(__builtin_ctz(word));
+        word &= word - 1;
+        const uint32_t v = x.bmbase + (w << 5) + bit;
+        if (v < g.V) flags[size_t(u) * g.V + old_of_new[v]] = 1;
+      }
+    }
+  }
+  return FSIG_OK;
+}
+
+}  // namespace fsig

@@ -1,0 +1,107 @@
+// Batch matching pipeline shared between the C ABI and the planner.
+#pragma once
+#include <stdint.h>
+
+#include <vector>
+
+#include "engine.h"
+
+namespace fsig {
+
+constexpr int kMaxQ = FSIG_MAX_QUERY;
+
+// Filter tests (bit flags).
+constexpr uint32_t kFilterDegree = 1u;
+constexpr uint32_t kFilterSignature = 2u;
+
+// Device order modes.
+constexpr uint32_t kOrderGSI = 0;      // candidate count, 0.9 decay of neighbours (match/GSI.cu:105-149)
+constexpr uint32_t kOrderMMatch = 1;   // core < forest < leaf offsets, then count (match/MMatch.cu:1575-1641)
+constexpr uint32_t kOrderScores = 2;   // externally supplied scores (learned), frontier argmin
+constexpr uint32_t kOrderGiven = 3;    // fixed order
+
+// One validated query, in host form.
+struct HostQuery {
+  uint32_t n = 0;
+  // neighbour lists in the caller's edge order (both directions, duplicates
+  // kept), as UndirectedPlainGraph::add_edge builds them (graph/graph.cc:23-33);
+  // the reference orders iterate these lists.
+  std::vector<std::vector<uint32_t>> nbr;
+  int32_t label[kMaxQ];
+  uint32_t adj[kMaxQ];   // neighbour bitmask (no self-loops, no duplicates)
+  uint32_t deg[kMaxQ];
+  uint32_t sig[kMaxQ][kSigWords];
+  uint32_t given[kMaxQ];
+  bool has_given = false;
+  int status = FSIG_OK;
+};
+
+int prepare_query(const fsig_query& q, int32_t num_labels, HostQuery& out);
+
+// Per-query-vertex descriptor on the device (16-byte aligned for the
+// vector loads of the signature).
+struct alignas(16) QVert {
+  uint32_t sig[kSigWords];
+  int32_t label;
+  uint32_t deg;
+  uint32_t adj;        // neighbours, as local ids of the same query
+  uint32_t q;          // query index in the batch
+  uint32_t u;          // local id
+  uint32_t words;      // bitmap words (0: no data vertex carries this label)
+  uint32_t bmbase;     // first new id covered by bitmap word 0 (multiple of 32)
+  uint32_t pad;
+  uint64_t bmoff;      // word offset of the bitmap in the pool
+};
+
+// Per-query matching plan, built on the device from the chosen order.
+struct Plan {
+  uint32_t n;
+  uint32_t ok;         // 0: some vertex has no candidate, nothing to enumerate
+  uint32_t g0;         // first query-vertex descriptor of this query
+  uint32_t pad;
+  uint32_t qv[kMaxQ];      // query vertex at position i
+  int32_t lab[kMaxQ];      // its label
+  uint32_t bwd[kMaxQ];     // positions j < i adjacent to position i
+  uint32_t same[kMaxQ];    // positions j < i with the same label
+  uint32_t bmbase[kMaxQ];
+  uint64_t bmoff[kMaxQ];
+};
+
+struct QueryResult {
+  unsigned long long count;
+  unsigned long long hash;
+  unsigned long long levels[kMaxQ];
+};
+
+struct BatchOptions {
+  uint32_t filter_mode = kFilterDegree | kFilterSignature;
+  int refine_iters = 0;
+  uint32_t order_mode = kOrderGSI;
+  uint32_t chunk = 4;        // root tasks per grab
+  uint32_t warps_per_block = 8;
+  const float* scores = nullptr;  // host scores per query vertex (kOrderScores), batch order
+  // When set, candidate counts are brought to the host after filtering and
+  // this function chooses each query's order (the reference-exact orders).
+  void (*host_order)(const HostQuery&, const uint32_t* cand, uint32_t* order) = nullptr;
+};
+
+struct BatchOutput {
+  std::vector<QueryResult> res;
+  std::vector<uint32_t> counts;    // candidates per query vertex (batch order)
+  std::vector<uint32_t> orders;    // kMaxQ per query
+  std::vector<uint32_t> ok;
+  float ms_filter = 0, ms_join = 0;
+  unsigned long long algo_bytes = 0;  // modelled bytes read by the enumerator
+};
+
+// Runs filter -> refine -> order -> roots -> enumerate for a batch.
+int run_batch(Engine& e, const std::vector<HostQuery>& qs, const BatchOptions& opt, BatchOutput& out);
+
+// Filter (+ refinement) only; flags[n*V] in caller vertex ids, for one query.
+int run_filter_probe(Engine& e, const HostQuery& q, uint32_t filter_mode, int refine_iters, uint8_t* flags);
+
+// Host-side reference orders (plan.cpp).
+void gsi_order_host(const HostQuery& q, const uint32_t* cand, uint32_t* order);
+void mmatch_order_host(const HostQuery& q, const uint32_t* cand, uint32_t* order);
+
+}  // namespace fsig

@@ -1,0 +1,247 @@
+// Host-side join orders with the reference's exact semantics, including its
+// std::priority_queue tie-breaking (same container, comparator and push
+// sequence), for the single-query path.  The batched path orders on the
+// device with the same scores and ties broken by the lowest vertex id.
+#include <algorithm>
+#include <cstring>
+#include <queue>
+#include <utility>
+#include <vector>
+
+#include "match.h"
+
+namespace fsig {
+namespace {
+
+// ScoredVertex (match/GSI.h:23-36): ordered by score only.
+struct Scored {
+  uint32_t id;
+  float score;
+  bool operator>(const Scored& o) const { return score > o.score; }
+};
+using MinQueue = std::priority_queue<Scored, std::vector<Scored>, std::greater<Scored>>;
+
+}  // namespace
+
+// GSI::generate_join_order (match/GSI.cu:105-149): start from the vertex with
+// the fewest candidates; each later position takes the frontier vertex with
+// the lowest score; the neighbours of each placed vertex have their score
+// multiplied by 0.9.
+void gsi_order_host(const HostQuery& q, const uint32_t* cand, uint32_t* order) {
+  const uint32_t n = q.n;
+  std::vector<Scored> qv(n);
+  std::vector<char> visited(n, 0);
+  for (uint32_t i = 0; i < n; i++) qv[i] = Scored{i, float(cand[i])};
+  for (uint32_t pos = 0; pos < n; pos++) {
+    MinQueue pq;
+    if (pos == 0) {
+      for (auto& s : qv) pq.push(s);
+    } else {
+      for (uint32_t j = 0; j < pos; j++)
+        for (uint32_t w : q.nbr[order[j]])
+          if (!visited[w]) pq.push(qv[w]);
+    }
+    const uint32_t u = pq.top().id;
+    order[pos] = u;
+    visited[u] = 1;
+    for (uint32_t w : q.nbr[u]) qv[w].score = float(double(qv[w].score) * 0.9);
+  }
+}
+
+namespace {
+
+// MMatch::decompose_query_graph (match/MMatch.cu:543-607): peel degree-1
+// vertices; 2 = 2-core, 1 = forest, 0 = leaf.
+std::vector<uint32_t> decompose(const HostQuery& q) {
+  const uint32_t n = q.n;
+  std::vector<uint32_t> d(n), type(n);
+  std::queue<uint32_t> leaves;
+  for (uint32_t i = 0; i < n; i++) {
+    d[i] = uint32_t(q.nbr[i].size());
+    if (d[i] == 1) leaves.push(i);
+  }
+  while (!leaves.empty()) {
+    const uint32_t v = leaves.front();
+    for (uint32_t w : q.nbr[v]) {
+      const uint32_t dw = d[w];
+      if (dw == 0) continue;
+      d[w]--;
+      if (dw == 2) leaves.push(w);
+    }
+    leaves.pop();
+    d[v] = 0;
+  }
+  for (uint32_t i = 0; i < n; i++) type[i] = d[i] >= 2 ? 2 : (q.nbr[i].size() == 1 ? 0 : 1);
+  return type;
+}
+
+// MMatch::find_equivalent_classes (match/MMatch.cu:34-173): classes of equal
+// (degree, label), split while no neighbour permutation maps classes and
+// labels onto each other.  The permutation search is the reference's
+// next_permutation walk from the current arrangement; it is skipped (the
+// vertices are treated as different) above degree 10, where the reference's
+// search would take minutes.
+struct Classes {
+  std::vector<std::vector<uint32_t>> members;
+  std::vector<std::pair<uint32_t, uint32_t>> inv;  // (class, index in class)
+};
+
+bool maps(const HostQuery& q, const std::vector<uint32_t>& a, const std::vector<uint32_t>& b,
+          const std::vector<std::pair<uint32_t, uint32_t>>& inv) {
+  for (size_t i = 0; i < a.size(); i++)
+    if (inv[a[i]].first != inv[b[i]].first || q.label[a[i]] != q.label[b[i]]) return false;
+  return true;
+}
+
+bool permutation_match(const HostQuery& q, const std::vector<uint32_t>& crt, std::vector<uint32_t> tgt,
+                       const std::vector<std::pair<uint32_t, uint32_t>>& inv) {
+  if (crt.size() != tgt.size() || crt.size() > 10) return false;
+  do {
+    if (maps(q, crt, tgt, inv)) return true;
+  } while (std::next_permutation(tgt.begin(), tgt.end()));
+  return false;
+}
+
+Classes equivalent_classes(const HostQuery& q) {
+  const uint32_t n = q.n;
+  Classes c;
+  c.members.push_back(std::vector<uint32_t>(1, 0));
+  c.inv.assign(n, {0, 0});
+  for (uint32_t i = 1; i < n; i++) {
+    bool eq = false;
+    for (uint32_t j = 0; j < c.members.size(); j++) {
+      const uint32_t r = c.members[j][0];
+      if (q.nbr[i].size() == q.nbr[r].size() && q.label[i] == q.label[r]) {
+        eq = true;
+        c.members[j].push_back(i);
+        c.inv[i] = {j, uint32_t(c.members[j].size() - 1)};
+      }
+    }
+    if (!eq) {
+      c.members.push_back(std::vector<uint32_t>(1, i));
+      c.inv[i] = {uint32_t(c.members.size() - 1), 0};
+    }
+  }
+  std::vector<uint32_t> checked;
+  for (auto& m : c.members)
+    for (size_t i = 1; i < m.size(); i++) checked.push_back(m[i]);
+  size_t old = c.members.size();
+  while (old != n && !checked.empty()) {
+    std::vector<uint32_t> next_checked;
+    for (uint32_t v : checked) {
+      if (c.members[c.inv[v].first].size() == 1) continue;
+      const uint32_t target = c.inv[v].second == 0 ? 1 : 0;
+      const std::vector<uint32_t>& crt = q.nbr[v];
+      bool eq = permutation_match(q, crt, q.nbr[c.members[c.inv[v].first][target]], c.inv);
+      if (!eq) {
+        std::vector<uint32_t> cls = c.members[c.inv[v].first];
+        cls.erase(cls.begin() + c.inv[v].second);
+        c.members[c.inv[v].first] = cls;
+        for (uint32_t i = 0; i < cls.size(); i++) c.inv[cls[i]] = {c.inv[v].first, i};
+        for (size_t i = old; i < c.members.size(); i++) {
+          if (q.label[v] != q.label[c.members[i][0]]) continue;
+          c.inv[v].first = uint32_t(i);
+          eq = permutation_match(q, crt, q.nbr[c.members[i][0]], c.inv);
+          if (eq) {
+            c.members[i].push_back(v);
+            c.inv[v].second = uint32_t(c.members[i].size() - 1);
+            break;
+          }
+        }
+        if (!eq) {
+          c.members.push_back(std::vector<uint32_t>(1, v));
+          c.inv[v] = {uint32_t(c.members.size() - 1), 0};
+        }
+        for (uint32_t w : crt)
+          if (std::find(next_checked.begin(), next_checked.end(), w) == next_checked.end()) next_checked.push_back(w);
+      }
+    }
+    old = c.members.size();
+    checked = next_checked;
+  }
+  return c;
+}
+
+// MMatch::compute_weight (match/MMatch.cu:270-296): BFS levels weighted by depth.
+double bfs_weight(const HostQuery& q, uint32_t root) {
+  std::vector<char> seen(q.n, 0);
+  seen[root] = 1;
+  uint32_t nseen = 1, level = 0;
+  double w = 0;
+  std::vector<uint32_t> frontier(1, root);
+  while (nseen < q.n) {
+    std::vector<uint32_t> next;
+    for (uint32_t v : frontier)
+      for (uint32_t x : q.nbr[v])
+        if (!seen[x]) { next.push_back(x); seen[x] = 1; }
+    if (next.empty()) break;
+    w += double(next.size()) * (level + 1);
+    level++;
+    nseen += uint32_t(next.size());
+    frontier = next;
+  }
+  return w;
+}
+
+}  // namespace
+
+// MMatch::generate_join_order (match/MMatch.cu:1575-1641).  Class candidate
+// counts are the counts of each class's first member.  Without a 2-core the
+// first position is restricted to the class of the forest vertex of least BFS
+// weight (select_min_spanning_tree, MMatch.cu:298-315).
+void mmatch_order_host(const HostQuery& q, const uint32_t* cand, uint32_t* order) {
+  const uint32_t n = q.n;
+  const std::vector<uint32_t> vtype = decompose(q);
+  const Classes c = equivalent_classes(q);
+  const uint32_t nc = uint32_t(c.members.size());
+  std::vector<uint32_t> ctype(nc), ccount(nc);
+  for (uint32_t i = 0; i < nc; i++) {
+    ctype[i] = vtype[c.members[i][0]];
+    ccount[i] = cand[c.members[i][0]];
+  }
+  float max_core = 0, max_forest = 0;
+  bool has_core = false;
+  for (uint32_t i = 0; i < nc; i++) {
+    if (ctype[i] == 2) has_core = true;
+    if (ctype[i] == 2 && float(ccount[i]) > max_core) max_core = float(ccount[i]);
+    else if (ctype[i] == 1 && float(ccount[i]) > max_forest) max_forest = float(ccount[i]);
+  }
+  uint32_t root_class = 0xffffffffu;
+  if (!has_core) {
+    double best = 0;
+    bool any = false;
+    uint32_t root = 0;
+    for (uint32_t i = 0; i < n; i++) {
+      if (vtype[i] != 1) continue;
+      double w = bfs_weight(q, i);
+      if (!any || w < best) { best = w; root = i; any = true; }
+    }
+    if (any) root_class = c.inv[root].first;
+  }
+  std::vector<Scored> qv(n);
+  for (uint32_t i = 0; i < n; i++) {
+    const uint32_t k = c.inv[i].first;
+    float s;
+    if (ctype[k] == 0) s = (float(ccount[k]) + max_forest) + max_core;
+    else if (ctype[k] == 1) s = float(ccount[k]) + max_core;
+    else s = float(ccount[k]);
+    qv[i] = Scored{i, s};
+  }
+  std::vector<char> visited(n, 0);
+  for (uint32_t pos = 0; pos < n; pos++) {
+    MinQueue pq;
+    if (pos == 0) {
+      for (uint32_t i = 0; i < n; i++)
+        if (root_class == 0xffffffffu || c.inv[i].first == root_class) pq.push(qv[i]);
+    } else {
+      for (uint32_t j = 0; j < pos; j++)
+        for (uint32_t w : q.nbr[order[j]])
+          if (!visited[w]) pq.push(qv[w]);
+    }
+    const uint32_t u = pq.top().id;
+    order[pos] = u;
+    visited[u] = 1;
+  }
+}
+
+}  // namespace fsig

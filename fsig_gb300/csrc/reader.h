@@ -1,0 +1,17 @@
+#pragma once
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+namespace fsig {
+
+struct TveGraph {
+  uint32_t num_vertices = 0;
+  std::vector<int32_t> labels;   // -1 for ids without a v record
+  std::vector<uint32_t> edges;   // pairs, file order
+};
+
+int read_tve(const char* path, int is_labeled, TveGraph& g, std::string& err);
+
+}  // namespace fsig

@@ -1,0 +1,138 @@
+/* FSIG-GB300: C ABI of the subgraph-matching engine (libfsig.so).
+ *
+ * This is the drop-in boundary for the reference's matching path.  Each entry
+ * point names the reference interface it replaces.  Conventions:
+ *   - opaque handles; every function returns an int status (FSIG_OK == 0,
+ *     negative on error) and never exits the process;
+ *   - the caller owns every host buffer; the engine owns one device arena;
+ *   - one engine per host thread (engines are independent; a single engine is
+ *     not safe to call from two threads at once);
+ *   - the engine runs only on the GPU: there is no CPU fallback.  A process
+ *     without a usable sm_103 device gets FSIG_ENODEV from fsig_create.
+ *
+ * Matching semantics (both algorithms, as in the reference): an embedding is
+ * an injective map f from query vertices to data vertices with
+ * label(f(u)) == label(u) and (u,w) in E(q) => (f(u),f(w)) in E(G); it is
+ * non-induced and automorphic images count separately
+ * (match/GSI_kernels.cuh:199-213, match/MMatch_kernels.cuh:641-654).  The data
+ * graph is matched as a simple graph: duplicate edges and self-loops are
+ * collapsed when it is loaded.
+ *
+ * Result hash: h(f) = fmix64(FSIG_HASH_SEED + sum_u fmix64((u << 32) | f(u)))
+ * with fmix64 the MurmurHash3 64-bit finaliser; the set hash is the sum of
+ * h(f) over all embeddings, modulo 2^64.  It does not depend on the order in
+ * which embeddings are found.
+ */
+#ifndef FSIG_H
+#define FSIG_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FSIG_HASH_SEED 0x46534947b3000001ull
+#define FSIG_MAX_QUERY 32
+
+/* status codes */
+#define FSIG_OK 0
+#define FSIG_EINVAL (-1)        /* bad argument                                  */
+#define FSIG_ENODEV (-2)        /* no usable CUDA device                         */
+#define FSIG_ECUDA (-3)         /* a CUDA call failed (see fsig_last_error)      */
+#define FSIG_EADMISSION (-4)    /* request does not fit the device arena         */
+#define FSIG_ENOGRAPH (-5)      /* no data graph loaded                          */
+#define FSIG_EQUERY (-6)        /* query too large, disconnected or malformed    */
+#define FSIG_EIO (-7)           /* file could not be read or parsed              */
+#define FSIG_ETIMEOUT (-8)      /* a bounded device wait gave up                 */
+#define FSIG_EOVERFLOW (-9)     /* a device work queue overflowed                */
+
+/* algorithms (argv[3] of the reference CLI, main/run.cc:31) */
+#define FSIG_ALGO_FSIG 1  /* label+degree filter, neighbour-support refinement, core/forest/leaf order (MMatch) */
+#define FSIG_ALGO_GSI 2   /* label+signature filter, candidate-count order with 0.9 decay (GSI)                  */
+#define FSIG_ALGO_FUSED 3 /* all filters + refinement, candidate-count order                                      */
+
+/* order sources */
+#define FSIG_ORDER_HEURISTIC 0 /* the algorithm's own order                         */
+#define FSIG_ORDER_LEARNED 1   /* the loaded order-scoring network (fsig_mpnn_*)    */
+#define FSIG_ORDER_GIVEN 2     /* fsig_query.order                                   */
+
+typedef struct fsig_engine fsig_engine;
+
+/* A query graph: n <= 32 vertices, m undirected edges (pairs of vertex ids). */
+typedef struct {
+  uint32_t num_vertices;
+  uint32_t num_edges;
+  const int32_t* labels;  /* [num_vertices]   */
+  const uint32_t* edges;  /* [2 * num_edges]  */
+  const uint32_t* order;  /* [num_vertices] or NULL; used with FSIG_ORDER_GIVEN */
+} fsig_query;
+
+typedef struct {
+  uint64_t count;                       /* number of embeddings (exact, 64-bit)        */
+  uint64_t hash;                        /* order-independent set hash                   */
+  int32_t status;                       /* FSIG_OK or the query's own error             */
+  uint32_t num_vertices;
+  uint32_t order[FSIG_MAX_QUERY];       /* matching order used (query vertex ids)      */
+  uint32_t candidates[FSIG_MAX_QUERY];  /* |C(u)| after filtering, by query vertex id   */
+  uint64_t level_counts[FSIG_MAX_QUERY];/* partial embeddings of length d+1, d=0..n-1   */
+  float ms_filter;                      /* device time: filter + refinement            */
+  float ms_join;                        /* device time: enumeration                    */
+} fsig_result;
+
+typedef struct {
+  int algo;            /* FSIG_ALGO_*                                     */
+  int order_source;    /* FSIG_ORDER_*                                    */
+  int refine_iters;    /* neighbour-support refinement steps (-1: default) */
+  int use_graph;       /* capture/replay the batch as one CUDA graph       */
+  uint32_t chunk;      /* root tasks taken per warp grab (0: autotuned)    */
+  uint32_t split_len;  /* level-1 driver range per task (0: autotuned)     */
+} fsig_batch_opts;
+
+/* ---- engine lifetime; replaces GPUSubgraphMatcher::init_GPU (match/subgraph_match.h:51-80)
+ *      and MemoryManager (memory_manager/memory_manager.h:16-265): one device arena of
+ *      arena_bytes (0 = a quarter of the device's memory), admission-checked. ---- */
+int fsig_create(int device, uint64_t arena_bytes, fsig_engine** out);
+int fsig_destroy(fsig_engine* e);
+const char* fsig_last_error(const fsig_engine* e);
+const char* fsig_status_string(int status);
+
+/* ---- data graph; replaces GraphReader::read (IO/graph_reader.h:27-34) followed by
+ *      GraphFormatTransformer::transform (graph_format_transformer/graph_format_transformer.h:37-40)
+ *      and MMatch::copy_graph_to_GPU (match/MMatch.cu:14-32).  The CSR, the
+ *      label-partitioned adjacency and the signature table are built on the device. ---- */
+int fsig_load_graph(fsig_engine* e, uint32_t num_vertices, const int32_t* labels,
+                    uint64_t num_edges, const uint32_t* edges);
+/* Reads a t/v/e file with the reference reader's semantics (graph_reader.cc:12-55);
+ * is_labeled == 0 sets every label to 0 (argv[4] of main/run.cc:32). */
+int fsig_load_graph_file(fsig_engine* e, const char* path, int is_labeled);
+int fsig_graph_info(const fsig_engine* e, uint32_t* num_vertices, uint64_t* num_adj,
+                    int32_t* num_labels, uint32_t* max_degree);
+
+/* ---- matching; replaces GPUSubgraphMatcher::match (match/subgraph_match.h:46),
+ *      i.e. MMatch::match (match/MMatch.cu:2077-2121, algo 1) and GSI::match
+ *      (match/GSI.cu:329-358, algo 2), for one query. ---- */
+int fsig_match(fsig_engine* e, const fsig_query* q, int algo, fsig_result* out);
+/* Many queries against the resident data graph in one persistent launch. */
+int fsig_match_batch(fsig_engine* e, uint32_t num_queries, const fsig_query* qs,
+                     const fsig_batch_opts* opts, fsig_result* out);
+
+/* ---- transforms with the reference's output layout, built on the device ---- */
+/* UndirectedPlainToCSRTransformer::transform (graph_format_transformer.cc:12-37):
+ * offsets[V+1], adj[2E]; rows ascending, duplicate edges kept as the reference keeps them. */
+int fsig_build_csr(fsig_engine* e, uint32_t num_vertices, uint64_t num_edges,
+                   const uint32_t* edges, uint32_t* offsets, uint32_t* adj);
+/* UndirectedPlainToPCSRTransformer::build_signature (graph_format_transformer.cc:217-281)
+ * over a CSR: 16 words per vertex; column-major [16][V] when column_oriented != 0. */
+int fsig_build_signature(fsig_engine* e, uint32_t num_vertices, const int32_t* labels,
+                         const uint32_t* offsets, const uint32_t* adj, int column_oriented,
+                         uint32_t* signature);
+
+/* ---- candidate filter probe: signature_filter (match/GSI.cu:34-103) and
+ *      kernel_initialise + refinement (match/MMatch.cu:609-1227) on the loaded graph.
+ *      flags[n * V] (1 = candidate), in the caller's vertex ids. ---- */
+int fsig_filter(fsig_engine* e, const fsig_query* q, int algo, int refine_iters, uint8_t* flags);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FSIG_H */
