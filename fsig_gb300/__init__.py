@@ -27,7 +27,8 @@ _BUILD = _PKG / "_build"
 HASH_SEED = 0x46534947B3000001
 MAX_QUERY = 32
 
-OK, EINVAL, ENODEV, ECUDA, EADMISSION, ENOGRAPH, EQUERY, EIO, ETIMEOUT, EOVERFLOW = 0, -1, -2, -3, -4, -5, -6, -7, -8, -9
+OK, EINVAL, ENODEV, ECUDA, EADMISSION, ENOGRAPH, EQUERY, EIO, ETIMEOUT, EOVERFLOW, ELIMIT = (
+    0, -1, -2, -3, -4, -5, -6, -7, -8, -9, -10)
 ALGO_FSIG, ALGO_GSI, ALGO_FUSED = 1, 2, 3
 ORDER_HEURISTIC, ORDER_LEARNED, ORDER_GIVEN = 0, 1, 2
 QUERY_INDUCED, QUERY_DENSE, QUERY_SPARSE = 0, 1, 2
@@ -52,7 +53,16 @@ class _Result(C.Structure):
 
 class _BatchOpts(C.Structure):
     _fields_ = [("algo", C.c_int), ("order_source", C.c_int), ("refine_iters", C.c_int), ("use_graph", C.c_int),
-                ("chunk", C.c_uint32), ("split_len", C.c_uint32)]
+                ("chunk", C.c_uint32), ("split_len", C.c_uint32), ("split_cycles", C.c_uint64),
+                ("max_work", C.c_uint64)]
+
+
+class _Stats(C.Structure):
+    _fields_ = [("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64), ("enum_bytes", C.c_uint64),
+                ("kernel_launches", C.c_uint32), ("enum_passes", C.c_uint32), ("ms_filter", C.c_float),
+                ("ms_join", C.c_float), ("ms_enum", C.c_float), ("pad", C.c_float), ("enum_tasks", C.c_uint64),
+                ("enum_pops", C.c_uint64), ("enum_handoffs", C.c_uint64), ("enum_records", C.c_uint64),
+                ("enum_examines", C.c_uint64)]
 
 
 _eng = None
@@ -94,7 +104,10 @@ def engine_library() -> C.CDLL:
     L.fsig_build_signature.argtypes = [vp, C.c_uint32, C.POINTER(C.c_int32), C.POINTER(C.c_uint32),
                                        C.POINTER(C.c_uint32), C.c_int, C.POINTER(C.c_uint32)]
     L.fsig_filter.argtypes = [vp, C.POINTER(_Query), C.c_int, C.c_int, C.POINTER(C.c_uint8)]
-    for name in ("fsig_create", "fsig_destroy", "fsig_load_graph", "fsig_load_graph_file", "fsig_graph_info",
+    L.fsig_plan_order.argtypes = [C.POINTER(_Query), C.c_int, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
+                                  C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
+    L.fsig_last_stats.argtypes = [vp, C.POINTER(_Stats)]
+    for name in ("fsig_last_stats", "fsig_plan_order", "fsig_create", "fsig_destroy", "fsig_load_graph", "fsig_load_graph_file", "fsig_graph_info",
                  "fsig_match", "fsig_match_batch", "fsig_build_csr", "fsig_build_signature", "fsig_filter"):
         getattr(L, name).restype = C.c_int
     _eng = L
@@ -120,6 +133,9 @@ def gen_library() -> C.CDLL:
     L.fsig_gen_query.argtypes = [C.c_uint32, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_int32),
                                  C.c_uint32, C.c_int, C.c_uint64, C.POINTER(C.c_int32), C.POINTER(C.c_uint32),
                                  C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
+    L.fsig_gen_query_ex.argtypes = [C.c_uint32, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_int32),
+                                    C.c_uint32, C.c_int, C.c_uint64, C.c_int32, C.POINTER(C.c_int32),
+                                    C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
     L.fsig_write_tve.argtypes = [C.c_char_p, C.c_uint32, C.POINTER(C.c_int32), C.c_uint64, C.POINTER(C.c_uint32)]
     _gen = L
     return L
@@ -258,7 +274,7 @@ def gen_labels(V: int, L: int, dist: str = "uniform", seed=1, s: float = 1.0) ->
     return lab
 
 
-def gen_query(g: Graph, n: int, mode: int = QUERY_INDUCED, seed: int = 1, csr=None) -> Query:
+def gen_query(g: Graph, n: int, mode: int = QUERY_INDUCED, seed: int = 1, csr=None, min_label: int = None) -> Query:
     off, adj = csr if csr is not None else g.csr()
     lab = np.ascontiguousarray(g.labels, np.int32)
     ql = np.zeros(n, np.int32)
@@ -266,11 +282,27 @@ def gen_query(g: Graph, n: int, mode: int = QUERY_INDUCED, seed: int = 1, csr=No
     m = C.c_uint32()
     src = np.zeros(n, np.uint32)
     adj = np.ascontiguousarray(adj if len(adj) else np.zeros(1, np.uint32), np.uint32)
-    rc = gen_library().fsig_gen_query(g.num_vertices, _u32p(off), _u32p(adj), _i32p(lab), n, mode, seed, _i32p(ql),
-                                      _u32p(qe), C.byref(m), _u32p(src))
+    if min_label is None:
+        rc = gen_library().fsig_gen_query(g.num_vertices, _u32p(off), _u32p(adj), _i32p(lab), n, mode, seed,
+                                          _i32p(ql), _u32p(qe), C.byref(m), _u32p(src))
+    else:
+        rc = gen_library().fsig_gen_query_ex(g.num_vertices, _u32p(off), _u32p(adj), _i32p(lab), n, mode, seed,
+                                             int(min_label), _i32p(ql), _u32p(qe), C.byref(m), _u32p(src))
     if rc:
         raise FsigError(rc, f"query extraction gave up (n={n}, mode={mode}, seed={seed})")
     return Query(ql, qe[: 2 * m.value].reshape(-1, 2).copy(), source=src)
+
+
+def gen_queries(g: Graph, specs, csr=None, threads: int = 0) -> list:
+    """Many queries at once: specs is a list of (n, mode, seed); extraction
+    runs on host threads (the generator library releases the GIL)."""
+    import concurrent.futures as cf
+    import os
+    csr = csr if csr is not None else g.csr()
+    threads = threads or min(32, os.cpu_count() or 4)
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        return list(ex.map(lambda s: gen_query(g, s[0], s[1], s[2], csr=csr,
+                                               min_label=s[3] if len(s) > 3 else None), specs))
 
 
 # ---------------------------------------------------------------------------
@@ -353,15 +385,22 @@ class Engine:
         return _result(r)
 
     def match_batch(self, qs: Sequence[Query], algo: int = ALGO_FUSED, order_source: int = ORDER_HEURISTIC,
-                    refine_iters: int = -1, chunk: int = 0, use_graph: bool = False) -> list:
+                    refine_iters: int = -1, chunk: int = 0, use_graph: bool = False, split_len: int = 0,
+                    split_cycles: int = 0, max_work: int = 0) -> list:
         keep = []
         arr = (_Query * max(len(qs), 1))()
         for i, q in enumerate(qs):
             arr[i] = _as_cquery(q, keep)
         res = (_Result * max(len(qs), 1))()
-        opts = _BatchOpts(algo, order_source, refine_iters, 1 if use_graph else 0, chunk, 0)
+        opts = _BatchOpts(algo, order_source, refine_iters, 1 if use_graph else 0, chunk, split_len, split_cycles,
+                          max_work)
         self._check(self._L.fsig_match_batch(self._h, len(qs), arr, C.byref(opts), res), "match_batch")
         return [_result(res[i]) for i in range(len(qs))]
+
+    def last_stats(self) -> dict:
+        st = _Stats()
+        self._check(self._L.fsig_last_stats(self._h, C.byref(st)), "last_stats")
+        return {k: getattr(st, k) for k, _ in _Stats._fields_ if k != "pad"}
 
     # transforms and filter probe
     def build_csr(self, V: int, edges: np.ndarray):
@@ -393,6 +432,37 @@ class Engine:
         self._check(self._L.fsig_filter(self._h, C.byref(cq), algo, refine_iters,
                                         out.ctypes.data_as(C.POINTER(C.c_uint8))), "filter")
         return out.reshape(q.num_vertices, V)
+
+
+def plan_order(q: Query, algo: int, candidates) -> dict:
+    """The reference-exact join order for given candidate counts (host only)."""
+    keep = []
+    cq = _as_cquery(q, keep)
+    n = q.num_vertices
+    cand = np.ascontiguousarray(candidates, np.uint32)
+    order = np.zeros(n, np.uint32)
+    types = np.zeros(n, np.uint32)
+    classes = np.zeros(n, np.uint32)
+    rc = engine_library().fsig_plan_order(C.byref(cq), algo, _u32p(cand), _u32p(order), _u32p(types),
+                                          _u32p(classes))
+    if rc:
+        raise FsigError(rc, "plan_order failed")
+    return dict(order=order.tolist(), types=types.tolist(), classes=classes.tolist())
+
+
+def select_within_budget(engine: "Engine", candidates: Sequence[Query], want: int, max_work: int,
+                         batch: int = 512, algo: int = ALGO_FUSED) -> list:
+    """The first `want` candidates, in order, whose enumeration under the
+    heuristic order examines at most `max_work` driver entries.  The choice
+    depends only on the queries and the data graph, not on scheduling."""
+    chosen = []
+    for i in range(0, len(candidates), batch):
+        part = list(candidates[i:i + batch])
+        rs = engine.match_batch(part, algo=algo, max_work=max_work)
+        chosen += [q for q, r in zip(part, rs) if r.status == OK]
+        if len(chosen) >= want:
+            break
+    return chosen[:want]
 
 
 class GPUSubgraphMatcher:

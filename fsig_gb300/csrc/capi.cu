@@ -49,9 +49,10 @@ int select(fsig_engine* h) {
 }
 
 void fill_result(const fsig::HostQuery& hq, const fsig::BatchOutput& o, uint32_t qi, uint32_t g0, fsig_result* r) {
-  r->count = o.res[qi].count;
-  r->hash = o.res[qi].hash;
-  r->status = FSIG_OK;
+  const bool over = o.res[qi].aborted != 0;
+  r->count = over ? 0 : o.res[qi].count;
+  r->hash = over ? 0 : o.res[qi].hash;
+  r->status = over ? FSIG_ELIMIT : FSIG_OK;
   r->num_vertices = hq.n;
   for (uint32_t i = 0; i < FSIG_MAX_QUERY; i++) {
     r->order[i] = i < hq.n ? o.orders[size_t(qi) * FSIG_MAX_QUERY + i] : 0;
@@ -73,7 +74,7 @@ void algo_options(int algo, int refine_iters, fsig::BatchOptions& o) {
     o.order_mode = fsig::kOrderGSI;
   } else {
     o.filter_mode = fsig::kFilterDegree | fsig::kFilterSignature;
-    o.refine_iters = refine_iters >= 0 ? refine_iters : 2;
+    o.refine_iters = refine_iters >= 0 ? refine_iters : 0;
     o.order_mode = fsig::kOrderGSI;
   }
 }
@@ -94,6 +95,7 @@ const char* fsig_status_string(int s) {
     case FSIG_EIO: return "file error";
     case FSIG_ETIMEOUT: return "device wait timed out";
     case FSIG_EOVERFLOW: return "device work queue overflow";
+    case FSIG_ELIMIT: return "query exceeded its work limit";
     default: return "unknown status";
   }
 }
@@ -139,6 +141,10 @@ int fsig_create(int device, uint64_t arena_bytes, fsig_engine** out) {
     err = cudaEventCreate(&ev);
     if (err != cudaSuccess) return bail(fsig::fail_cuda(err, "cudaEventCreate", __FILE__, __LINE__));
   }
+  for (auto& ev : e.ev_enum) {
+    err = cudaEventCreate(&ev);
+    if (err != cudaSuccess) return bail(fsig::fail_cuda(err, "cudaEventCreate", __FILE__, __LINE__));
+  }
   uint64_t bytes = arena_bytes ? arena_bytes : uint64_t(prop.totalGlobalMem) / 4;
   err = cudaMalloc(&e.arena.base, bytes);
   if (err != cudaSuccess) return bail(fsig::fail(FSIG_EADMISSION, "cannot reserve the device arena"));
@@ -153,6 +159,8 @@ int fsig_destroy(fsig_engine* h) {
   cudaSetDevice(h->e.device);
   if (h->e.stream) cudaStreamSynchronize(h->e.stream);
   for (auto& ev : h->e.ev)
+    if (ev) cudaEventDestroy(ev);
+  for (auto& ev : h->e.ev_enum)
     if (ev) cudaEventDestroy(ev);
   if (h->e.arena.base) cudaFree(h->e.arena.base);
   if (h->e.pinned) cudaFreeHost(h->e.pinned);
@@ -219,7 +227,7 @@ int fsig_match_batch(fsig_engine* h, uint32_t nq, const fsig_query* qs, const fs
   int rc = select(h);
   if (rc) return finish(h, rc);
   if ((nq && (!qs || !out))) return finish(h, fsig::fail(FSIG_EINVAL, "null argument"));
-  fsig_batch_opts def{FSIG_ALGO_FUSED, FSIG_ORDER_HEURISTIC, -1, 0, 0, 0};
+  fsig_batch_opts def{FSIG_ALGO_FUSED, FSIG_ORDER_HEURISTIC, -1, 0, 0, 0, 0, 0};
   const fsig_batch_opts& bo = opts ? *opts : def;
   if (bo.algo != FSIG_ALGO_FSIG && bo.algo != FSIG_ALGO_GSI && bo.algo != FSIG_ALGO_FUSED)
     return finish(h, fsig::fail(FSIG_EINVAL, "unknown algorithm"));
@@ -240,6 +248,9 @@ int fsig_match_batch(fsig_engine* h, uint32_t nq, const fsig_query* qs, const fs
   if (bo.order_source == FSIG_ORDER_GIVEN) o.order_mode = fsig::kOrderGiven;
   else if (bo.order_source == FSIG_ORDER_LEARNED) return finish(h, fsig::fail(FSIG_EINVAL, "no order network loaded"));
   if (bo.chunk) o.chunk = bo.chunk;
+  if (bo.split_len) o.split = bo.split_len;
+  if (bo.split_cycles) o.budget_cycles = (long long)bo.split_cycles;
+  o.max_work = bo.max_work;
   fsig::BatchOutput out_b;
   rc = fsig::run_batch(h->e, hq, o, out_b);
   if (rc) return finish(h, rc);
@@ -247,6 +258,30 @@ int fsig_match_batch(fsig_engine* h, uint32_t nq, const fsig_query* qs, const fs
   for (size_t k = 0; k < hq.size(); k++) {
     fill_result(hq[k], out_b, uint32_t(k), g0, &out[idx[k]]);
     g0 += hq[k].n;
+  }
+  return FSIG_OK;
+}
+
+int fsig_last_stats(const fsig_engine* h, fsig_batch_stats* out) {
+  if (!h || !out) return FSIG_EINVAL;
+  *out = h->e.last;
+  return FSIG_OK;
+}
+
+int fsig_plan_order(const fsig_query* q, int algo, const uint32_t* cand, uint32_t* order, uint32_t* types,
+                    uint32_t* classes) {
+  fsig::clear_thread_error();
+  if (!q || !cand || !order) return FSIG_EINVAL;
+  fsig::HostQuery hq;
+  int rc = fsig::prepare_query(*q, 0, hq);
+  if (rc) return rc;
+  if (algo == FSIG_ALGO_FSIG) {
+    fsig::mmatch_order_host(hq, cand, order);
+    fsig::mmatch_structure(hq, types, classes);
+  } else if (algo == FSIG_ALGO_GSI || algo == FSIG_ALGO_FUSED) {
+    fsig::gsi_order_host(hq, cand, order);
+  } else {
+    return FSIG_EINVAL;
   }
   return FSIG_OK;
 }

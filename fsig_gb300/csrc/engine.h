@@ -27,6 +27,7 @@ struct DeviceGraph {
   uint32_t* base = nullptr;        // [L+1] first new id of each label class
   uint32_t* off = nullptr;         // [V+1]
   uint32_t* adj = nullptr;         // [nadj] new ids, rows ascending, no duplicates
+  uint32_t* adj_old = nullptr;     // [nadj] caller id of each adj entry (for the result hash)
   uint32_t* lseg = nullptr;        // [V*(L+1)]
   uint4* sig = nullptr;            // [V*4] 64-byte signature per vertex
   std::vector<uint32_t> h_base;    // host copy of base
@@ -44,8 +45,14 @@ struct Engine {
   // pinned host staging for batches
   void* pinned = nullptr;
   uint64_t pinned_bytes = 0;
+  // enumeration kernel: resident blocks per SM (0 until first queried)
+  int enum_per_sm = 0;
   // timing events
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t ev_enum[2] = {nullptr, nullptr};
+  fsig_batch_stats last{};
+  uint64_t cur_h2d = 0;  // host-to-device bytes of the call in progress
+  unsigned long long last_ev[8] = {0};  // enumeration event counters of the last call
 };
 
 // graph_store.cu

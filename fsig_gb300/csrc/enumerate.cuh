@@ -1,0 +1,552 @@
+// Enumeration kernel: depth-first extension of partial embeddings, one warp
+// per task, with work stealing.  Included by match.cu.
+//
+// A task is (query q, depth d, mapped vertices f[0..d), driver range
+// [lo, hi) at depth d).  Pass 0 takes implicit tasks: every root candidate of
+// every query, with its depth-1 driver range cut into chunks of `split`
+// entries.  Later passes (normally none) take explicit task records.
+//
+// Level state lives in registers distributed over lanes: lane j holds, for
+// depth j, the mapped vertex f_j, the partial hash S_j (sum of fmix64 terms of
+// depths 0..j), the driver cursor (dpos_j, dend_j, drv_j) and the candidate
+// buffer cursor (cnt_j, it_j).  The candidate buffers (32 per depth) and the
+// current query's plan are in shared memory.
+//
+// Candidates at depth i come from the driver -- the shortest label-l(i)
+// segment among the rows of the backward neighbours -- 32 entries at a time,
+// one per lane, filtered by injectivity (against earlier same-label depths),
+// the candidate bitmap of depth i, and membership in every other backward
+// segment.  For membership the warp finds the window of that segment spanned
+// by the 32 driver entries with a 32-ary search (all lanes probe 32 pivots per
+// round, about log32 of the segment length rounds); a window of at most 32
+// entries is then loaded once and searched in registers by shuffles, a longer
+// one by a per-lane binary search inside the window.
+//
+// Work stealing: warps that run out of input wait for work.  A busy warp
+// checks every 64 steps whether idle warps outnumber the queued records; if
+// so it hands its shallowest pending depth (buffered candidates and the
+// remaining driver range) to the queue as task records and carries on with
+// the rest.  Waiting is bounded: a warp that waits too long simply leaves,
+// which never loses work -- records still queued when the pass ends are the
+// next pass's input.  Every value that steers a warp's control flow is read
+// by lane 0 and broadcast.
+#pragma once
+
+namespace fsig {
+namespace {
+
+struct TaskRec {
+  uint32_t f[kMaxQ];
+  uint32_t q, d, lo, hi;  // lo == hi == kInvalid: the whole driver range
+};
+
+struct EnumArgs {
+  GraphView g;
+  const Plan* __restrict__ plans;
+  const uint32_t* __restrict__ pool;
+  uint32_t Q;
+  // pass-0 implicit tasks
+  const uint32_t* __restrict__ roots;
+  const uint32_t* __restrict__ root_q;
+  const uint32_t* __restrict__ chunk_off;  // [nroots + 1]
+  uint32_t nroots;
+  uint32_t split;
+  // explicit input tasks (passes >= 1)
+  const TaskRec* __restrict__ in_tasks;
+  uint32_t in_count;
+  // work queue
+  TaskRec* out_tasks;
+  uint32_t* out_ready;
+  uint32_t out_cap;
+  uint32_t tag;
+  uint32_t* ctr;  // counters, kCtrStride apart: [0] input grab, [1] queue tail (reserved),
+                  // [2] queue head, [3] error bits, [4] idle warps, [5] active warps
+  uint32_t chunk;
+  long long budget;  // cycles on a task before it may be split while warps are idle
+  QueryResult* res;
+  unsigned long long work_cap;  // per-query limit on examined driver entries (0: none)
+  unsigned long long* algo_bytes;
+  unsigned long long* ev;       // event counters: tasks, records popped, hand-offs, records written, examines
+  unsigned long long seed;
+};
+
+constexpr uint32_t kErrTimeout = 1u;
+constexpr uint32_t kCtrStride = 32;        // one 128-byte line per counter
+constexpr uint32_t kMaxWaiters = 2048;     // warps beyond this many idle ones leave instead of waiting
+constexpr uint32_t kReadySpinLimit = 1u << 22;
+constexpr uint32_t kIdleSpinLimit = 1u << 22;
+
+struct WarpSmem {
+  Plan plan;
+  uint32_t cand[kMaxQ][kChunk];
+};
+
+__device__ __forceinline__ bool bsearch_range(const uint32_t* __restrict__ a, uint32_t lo, uint32_t hi, uint32_t x,
+                                              unsigned long long& bytes) {
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    const uint32_t y = __ldg(a + mid);
+    bytes += 4;
+    if (y < x) lo = mid + 1;
+    else if (y > x) hi = mid;
+    else return true;
+  }
+  return false;
+}
+
+// First index in [lo, hi) of sorted a[] with a[i] >= key (warp-uniform key
+// and range): 32 pivots per round, then one 32-entry tile.
+__device__ __forceinline__ uint32_t warp_lower_bound(const uint32_t* __restrict__ a, uint32_t lo, uint32_t hi,
+                                                     uint32_t key, uint32_t lane, unsigned long long& bytes) {
+  while (hi - lo > 32) {
+    const uint32_t step = (hi - lo + 31) >> 5;
+    const uint32_t idx = lo + lane * step;
+    const bool in = idx < hi;
+    const uint32_t v = in ? __ldg(a + idx) : 0xffffffffu;
+    if (in) bytes += 4;
+    const uint32_t t = __popc(__ballot_sync(kFull, in && v < key));
+    if (t == 0) return lo;
+    const uint32_t nlo = lo + (t - 1) * step + 1;
+    const uint32_t nhi = min(hi, lo + t * step);
+    lo = nlo;
+    hi = nhi;
+  }
+  const uint32_t idx = lo + lane;
+  const bool in = idx < hi;
+  const uint32_t v = in ? __ldg(a + idx) : 0xffffffffu;
+  if (in) bytes += 4;
+  return lo + __popc(__ballot_sync(kFull, in && v < key));
+}
+
+__global__ void __launch_bounds__(256) enumerate_kernel(EnumArgs A) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  WarpSmem& ws = reinterpret_cast<WarpSmem*>(smem_raw)[threadIdx.x >> 5];
+  const uint32_t lane = threadIdx.x & 31;
+  const GraphView& g = A.g;
+  const uint64_t W1 = uint64_t(g.L) + 1;
+  const uint32_t T_in = A.in_tasks ? A.in_count : A.chunk_off[A.nroots];
+
+  // lane-distributed level state
+  uint32_t f = 0, dpos = 0, dend = 0, drv = 0, cnt = 0, it = 0;
+  unsigned long long S = 0, lc = 0;
+  unsigned long long my_count = 0, my_hash = 0, bytes = 0;
+  unsigned long long pend = 0;  // driver entries examined, not yet published to res.work (lane 0)
+  unsigned long long n_tasks = 0, n_pops = 0, n_handoffs = 0, n_recs = 0, n_examine = 0;  // lane 0
+  uint32_t cur_q = kInvalid;
+
+  auto flush = [&]() {
+    if (cur_q == kInvalid) return;
+    const unsigned long long c = warp_sum(my_count), h = warp_sum(my_hash);
+    if (lane == 0 && (c | h)) {
+      atomicAdd(&A.res[cur_q].count, c);
+      atomicAdd(&A.res[cur_q].hash, h);
+    }
+    if (lane < ws.plan.n && lc) atomicAdd(&A.res[cur_q].levels[lane], lc);
+    my_count = my_hash = 0;
+    lc = 0;
+  };
+
+  // Publishes the driver entries this warp examined for the current query and
+  // reports (warp-uniformly) whether the query is over its limit.  The total
+  // a query examines does not depend on how its work was split (ranges are
+  // cut at multiples of 32 from the same origins), so whether it exceeds the
+  // limit does not either.
+  auto over_limit = [&]() -> bool {
+    if (!A.work_cap) return false;
+    int stop = 0;
+    if (lane == 0) {
+      if (pend) {
+        const unsigned long long tot = atomicAdd(&A.res[cur_q].work, pend) + pend;
+        pend = 0;
+        if (tot > A.work_cap) atomicExch(&A.res[cur_q].aborted, 1u);
+      }
+      stop = *(volatile unsigned int*)&A.res[cur_q].aborted != 0;
+    }
+    return __shfl_sync(kFull, stop, 0) != 0;
+  };
+
+  auto use_query = [&](uint32_t q) {
+    if (q == cur_q) return;
+    if (cur_q != kInvalid) over_limit();  // publish the previous query's work
+    flush();
+    __syncwarp();
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(A.plans + q);
+    uint32_t* dst = reinterpret_cast<uint32_t*>(&ws.plan);
+    for (uint32_t i = lane; i < sizeof(Plan) / 4; i += 32) dst[i] = src[i];
+    __syncwarp();
+    cur_q = q;
+  };
+
+  // Driver of depth lv from the backward neighbours' rows; stored in lane lv.
+  auto enter = [&](uint32_t lv, uint32_t lo_set, uint32_t hi_set) {
+    const uint32_t bw = ws.plan.bwd[lv];
+    const int32_t lab = ws.plan.lab[lv];
+    uint32_t lo = 0, hi = 0, len = kInvalid;
+    if ((bw >> lane) & 1u) {
+      const uint32_t* s = g.lseg + uint64_t(f) * W1 + lab;
+      lo = s[0];
+      hi = s[1];
+      len = hi - lo;
+      bytes += 8;
+    }
+    const bool empty = __ballot_sync(kFull, len == 0) != 0;
+    const uint32_t j = warp_argmin(float(len), len == kInvalid ? 0xffffu : lane) & 31u;
+    const uint32_t dlo = __shfl_sync(kFull, lo, j), dhi = __shfl_sync(kFull, hi, j);
+    if (lane == lv) {
+      if (lo_set != kInvalid) {
+        dpos = lo_set;
+        dend = hi_set;
+      } else {
+        dpos = dlo;
+        dend = empty ? dlo : dhi;
+      }
+      drv = j;
+      cnt = 0;
+      it = 0;
+    }
+  };
+
+  // Examines the next 32 driver entries of depth lv.  x: candidate (new id);
+  // xo (leaf only): its caller id.
+  auto examine = [&](uint32_t lv, bool leaf, uint32_t& x, uint32_t& xo) -> bool {
+    const uint32_t dp = __shfl_sync(kFull, dpos, lv), de = __shfl_sync(kFull, dend, lv);
+    const uint32_t dv = __shfl_sync(kFull, drv, lv);
+    const int32_t lab = ws.plan.lab[lv];
+    uint32_t bw = ws.plan.bwd[lv] & ~(1u << dv);
+    uint32_t my_lo = 0, my_hi = 0;
+    if ((bw >> lane) & 1u) {
+      const uint32_t* s = g.lseg + uint64_t(f) * W1 + lab;
+      my_lo = s[0];
+      my_hi = s[1];
+      bytes += 8;
+    }
+    const uint32_t nvalid = min(32u, de - dp);
+    const uint32_t k = dp + lane;
+    bool pred = lane < nvalid;
+    x = pred ? __ldg(g.adj + k) : 0xffffffffu;
+    xo = (pred && leaf) ? __ldg(g.adj_old + k) : 0u;
+    if (pred) bytes += leaf ? 8 : 4;
+    // candidate bitmap of depth lv, issued before the window searches
+    uint32_t bmw = 0;
+    const uint32_t bit = x - ws.plan.bmbase[lv];
+    if (pred) {
+      bmw = __ldg(A.pool + ws.plan.bmoff[lv] + (bit >> 5));
+      bytes += 4;
+    }
+    uint32_t sm = ws.plan.same[lv];
+    while (sm) {
+      const uint32_t j = __ffs(sm) - 1;
+      sm &= sm - 1;
+      const uint32_t fj = __shfl_sync(kFull, f, j);
+      pred = pred && x != fj;
+    }
+    if (bw) {
+      const uint32_t xfirst = __shfl_sync(kFull, x, 0), xlast = __shfl_sync(kFull, x, nvalid - 1);
+      while (bw) {
+        const uint32_t j = __ffs(bw) - 1;
+        bw &= bw - 1;
+        const uint32_t lo = __shfl_sync(kFull, my_lo, j), hi = __shfl_sync(kFull, my_hi, j);
+        const uint32_t a = warp_lower_bound(g.adj, lo, hi, xfirst, lane, bytes);
+        const uint32_t b = warp_lower_bound(g.adj, a, hi, xlast + 1, lane, bytes);
+        const uint32_t w = b - a;
+        if (w == 0) {
+          pred = false;
+        } else if (w <= 32) {
+          const uint32_t tile = lane < w ? __ldg(g.adj + a + lane) : 0xffffffffu;
+          bytes += lane < w ? 4 : 0;
+          uint32_t l2 = 0, h2 = w;
+#pragma unroll
+          for (int step = 0; step < 6; step++) {
+            const uint32_t mid = (l2 + h2) >> 1;
+            const uint32_t v = __shfl_sync(kFull, tile, mid & 31);
+            if (l2 < h2) {
+              if (v < x) l2 = mid + 1; else h2 = mid;
+            }
+          }
+          const uint32_t v = __shfl_sync(kFull, tile, l2 & 31);
+          pred = pred && l2 < w && v == x;
+        } else if (pred) {
+          pred = bsearch_range(g.adj, a, b, x, bytes);
+        }
+        if (__ballot_sync(kFull, pred) == 0) break;
+      }
+    }
+    pred = pred && ((bmw >> (bit & 31)) & 1u);
+    if (lane == lv) dpos = dp + kChunk;
+    if (lane == 0) {
+      n_examine++;
+      pend += nvalid;
+    }
+    return pred;
+  };
+
+  // Hands the shallowest depth in [d0, lv] that still has work (buffered
+  // candidates and the rest of its driver range) to the queue and marks that
+  // depth done here.  Returns false when the queue has no room.
+  auto donate = [&](uint32_t d0, uint32_t lv) -> bool {
+    const uint32_t n = ws.plan.n;
+    uint32_t mine = 0;
+    if (lane >= d0 && lane <= lv) {
+      if (lane + 1 < n && cnt > it) mine += cnt - it;
+      if (dend > dpos) mine += (dend - dpos + A.split - 1) / A.split;
+    }
+    const uint32_t has = __ballot_sync(kFull, mine > 0);
+    if (!has) return true;
+    const uint32_t l = __ffs(has) - 1;
+    const uint32_t total = __shfl_sync(kFull, mine, l);
+    uint32_t base = 0;
+    if (lane == 0) {
+      base = kInvalid;
+      uint32_t r = *(volatile uint32_t*)&A.ctr[1 * kCtrStride];
+      while (r + total <= A.out_cap) {
+        const uint32_t prev = atomicCAS(&A.ctr[1 * kCtrStride], r, r + total);
+        if (prev == r) { base = r; break; }
+        r = prev;
+      }
+    }
+    base = __shfl_sync(kFull, base, 0);
+    if (base == kInvalid) return false;
+    uint32_t slot = base;
+    const uint32_t c_l = __shfl_sync(kFull, cnt, l), i_l = __shfl_sync(kFull, it, l);
+    const uint32_t p_l = __shfl_sync(kFull, dpos, l), e_l = __shfl_sync(kFull, dend, l);
+    if (l + 1 < n) {
+      for (uint32_t k = i_l; k < c_l; k++) {
+        TaskRec* r = A.out_tasks + slot++;
+        const uint32_t cv = ws.cand[l][k];
+        if (lane < l) r->f[lane] = f;
+        if (lane == l) r->f[lane] = cv;
+        if (lane == 0) { r->q = cur_q; r->d = l + 1; r->lo = kInvalid; r->hi = kInvalid; }
+      }
+    }
+    for (uint32_t p = p_l; p < e_l; p += A.split) {
+      TaskRec* r = A.out_tasks + slot++;
+      if (lane < l) r->f[lane] = f;
+      if (lane == 0) { r->q = cur_q; r->d = l; r->lo = p; r->hi = min(p + A.split, e_l); }
+    }
+    if (lane == l) {
+      it = cnt;
+      dpos = dend;
+    }
+    __threadfence();
+    __syncwarp();
+    for (uint32_t s = base + lane; s < base + total; s += 32) atomicExch(&A.out_ready[s], A.tag);
+    if (lane == 0) { n_handoffs++; n_recs += total; }
+    return true;
+  };
+
+  // Whether idle warps are waiting for more work than the queue holds.
+  // Decided by lane 0 alone and broadcast.
+  auto should_split = [&](long long t_start) -> bool {
+    int w = 0;
+    if (lane == 0 && A.out_cap) {
+      const uint32_t idle = *(volatile uint32_t*)&A.ctr[4 * kCtrStride];
+      if (idle) {
+        const uint32_t tail = *(volatile uint32_t*)&A.ctr[1 * kCtrStride], head = *(volatile uint32_t*)&A.ctr[2 * kCtrStride];
+        w = (tail - min(head, tail) < idle) && clock64() - t_start > A.budget;
+      }
+    }
+    return __shfl_sync(kFull, w, 0) != 0;
+  };
+
+  // Runs one task: depth d, mapped f (lane-distributed, lanes < d), driver
+  // range override [lo, hi) at depth d.
+  auto run = [&](uint32_t d, uint32_t lo_set, uint32_t hi_set) {
+    const uint32_t n = ws.plan.n;
+    if (lane == 0) n_tasks++;
+    // partial hashes of depths < d by an inclusive warp scan of the terms
+    unsigned long long term = 0;
+    if (lane < d) {
+      term = fmix64((uint64_t(ws.plan.qv[lane]) << 32) | __ldg(g.old_of_new + f));
+      bytes += 4;
+    }
+    unsigned long long incl = term;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned long long y = __shfl_up_sync(kFull, incl, o);
+      if (lane >= uint32_t(o)) incl += y;
+    }
+    S = incl;
+    if (d == n) {  // a complete embedding (single-vertex queries)
+      const unsigned long long Sn = __shfl_sync(kFull, S, n - 1);
+      if (lane == 0) {
+        my_count += 1;
+        my_hash += fmix64(A.seed + Sn);
+      }
+      return;
+    }
+    if (A.work_cap && over_limit()) return;
+    const long long t_start = clock64();
+    uint32_t lv = d;
+    enter(d, lo_set, hi_set);
+    uint32_t steps = 0;
+    while (true) {
+      if ((++steps & 63u) == 0) {
+        if (over_limit()) return;
+        if (should_split(t_start)) donate(d, lv);
+      }
+      if (lv == n - 1) {
+        const unsigned long long Sp = __shfl_sync(kFull, S, lv - 1);
+        const uint64_t tb = uint64_t(ws.plan.qv[lv]) << 32;
+        while (__shfl_sync(kFull, dpos, lv) < __shfl_sync(kFull, dend, lv)) {
+          uint32_t x, xo;
+          const bool p = examine(lv, true, x, xo);
+          const uint32_t m = __ballot_sync(kFull, p);
+          if (p) {
+            my_count += 1;
+            my_hash += fmix64(A.seed + Sp + fmix64(tb | xo));
+          }
+          if (lane == lv) lc += __popc(m);
+          if ((++steps & 63u) == 0) {
+            if (over_limit()) return;
+            if (should_split(t_start)) donate(d, lv);
+          }
+        }
+        if (lv == d) return;
+        lv--;
+        continue;
+      }
+      const uint32_t i = __shfl_sync(kFull, it, lv), c = __shfl_sync(kFull, cnt, lv);
+      if (i < c) {
+        const uint32_t x = ws.cand[lv][i];
+        const unsigned long long Sp = __shfl_sync(kFull, S, lv - 1);
+        if (lane == lv) {
+          it = i + 1;
+          f = x;
+          S = Sp + fmix64((uint64_t(ws.plan.qv[lv]) << 32) | __ldg(g.old_of_new + x));
+          bytes += 4;
+        }
+        lv++;
+        enter(lv, kInvalid, kInvalid);
+        continue;
+      }
+      if (__shfl_sync(kFull, dpos, lv) < __shfl_sync(kFull, dend, lv)) {
+        uint32_t x, xo;
+        const bool p = examine(lv, false, x, xo);
+        const uint32_t m = __ballot_sync(kFull, p);
+        __syncwarp();
+        if (p) ws.cand[lv][__popc(m & lanemask_lt())] = x;
+        __syncwarp();
+        if (lane == lv) {
+          cnt = __popc(m);
+          it = 0;
+          lc += __popc(m);
+        }
+        continue;
+      }
+      if (lv == d) return;
+      lv--;
+    }
+  };
+
+  // The header is read by lane 0 and broadcast, like every other value that
+  // steers the warp's control flow; records popped in this launch were
+  // written by another SM, so they are read through L2 (ld.cg).
+  auto run_record = [&](const TaskRec* r) {
+    uint32_t q = 0, d = 0, lo = 0, hi = 0;
+    if (lane == 0) {
+      q = __ldcg(&r->q);
+      d = __ldcg(&r->d);
+      lo = __ldcg(&r->lo);
+      hi = __ldcg(&r->hi);
+    }
+    q = __shfl_sync(kFull, q, 0);
+    d = __shfl_sync(kFull, d, 0);
+    lo = __shfl_sync(kFull, lo, 0);
+    hi = __shfl_sync(kFull, hi, 0);
+    use_query(q);
+    if (lane < d) f = __ldcg(&r->f[lane]);
+    run(d, lo, hi);
+  };
+
+  for (;;) {
+    // 1. input tasks
+    uint32_t t0 = T_in;
+    if (lane == 0 && *(volatile uint32_t*)&A.ctr[0 * kCtrStride] < T_in) t0 = atomicAdd(&A.ctr[0 * kCtrStride], A.chunk);
+    t0 = __shfl_sync(kFull, t0, 0);
+    if (t0 < T_in) {
+      const uint32_t t1 = min(t0 + A.chunk, T_in);
+      for (uint32_t t = t0; t < t1; t++) {
+        if (A.in_tasks) {
+          run_record(A.in_tasks + t);
+        } else {
+          // implicit: root i, chunk c of its depth-1 driver range
+          uint32_t lo = 0, hi = A.nroots;  // last i with chunk_off[i] <= t
+          while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (A.chunk_off[mid] <= t) lo = mid; else hi = mid;
+          }
+          const uint32_t i = lo, c = t - A.chunk_off[i];
+          use_query(A.root_q[i]);
+          const uint32_t r = A.roots[i];
+          if (lane == 0) f = r;
+          if (ws.plan.n == 1) {
+            run(1, kInvalid, kInvalid);
+          } else {
+            const uint32_t* s = g.lseg + uint64_t(r) * W1 + ws.plan.lab[1];
+            const uint32_t b0 = s[0], e0 = s[1];
+            const uint32_t clo = b0 + c * A.split;
+            if (lane == 0) lc += (c == 0);  // the root itself, once
+            run(1, clo, min(clo + A.split, e0));
+          }
+        }
+      }
+      continue;
+    }
+    // 2. input exhausted: take queued records, waiting while others work
+    uint32_t slot = kInvalid;
+    if (lane == 0) {
+      atomicSub(&A.ctr[5 * kCtrStride], 1u);
+      const uint32_t waiting = atomicAdd(&A.ctr[4 * kCtrStride], 1u);
+      uint32_t sleep_ns = 256;
+      // enough warps already wait: leave (queued work is never lost)
+      const uint32_t limit = waiting >= kMaxWaiters ? 1u : kIdleSpinLimit;
+      for (uint32_t spin = 0; spin < limit; spin++) {
+        const uint32_t tail = min(*(volatile uint32_t*)&A.ctr[1 * kCtrStride], A.out_cap);
+        uint32_t h = *(volatile uint32_t*)&A.ctr[2 * kCtrStride];
+        bool got = false;
+        while (h < tail) {
+          const uint32_t prev = atomicCAS(&A.ctr[2 * kCtrStride], h, h + 1);
+          if (prev == h) { slot = h; got = true; break; }
+          h = prev;
+        }
+        if (got) break;
+        // finished when nobody works and nothing is queued (active read first)
+        if (*(volatile uint32_t*)&A.ctr[5 * kCtrStride] == 0 &&
+            *(volatile uint32_t*)&A.ctr[2 * kCtrStride] >= min(*(volatile uint32_t*)&A.ctr[1 * kCtrStride], A.out_cap))
+          break;
+        if (spin + 1 == limit) break;
+        __nanosleep(sleep_ns);
+        if (sleep_ns < 8192) sleep_ns <<= 1;
+      }
+      atomicSub(&A.ctr[4 * kCtrStride], 1u);
+      if (slot != kInvalid) {
+        atomicAdd(&A.ctr[5 * kCtrStride], 1u);
+        uint32_t spins = 0;
+        while (*(volatile uint32_t*)&A.out_ready[slot] != A.tag) {
+          if (++spins > kReadySpinLimit) { atomicOr(&A.ctr[3 * kCtrStride], kErrTimeout); slot = kInvalid - 1; break; }
+          __nanosleep(64);
+        }
+        if (slot == kInvalid - 1) atomicSub(&A.ctr[5 * kCtrStride], 1u);
+      }
+    }
+    slot = __shfl_sync(kFull, slot, 0);
+    if (slot >= kInvalid - 1) break;
+    __threadfence();
+    if (lane == 0) n_pops++;
+    run_record(A.out_tasks + slot);
+  }
+  if (cur_q != kInvalid) over_limit();
+  flush();
+  bytes = warp_sum(bytes);
+  if (lane == 0) {
+    atomicAdd(A.algo_bytes, bytes);
+    atomicAdd(&A.ev[0], n_tasks);
+    atomicAdd(&A.ev[1], n_pops);
+    atomicAdd(&A.ev[2], n_handoffs);
+    atomicAdd(&A.ev[3], n_recs);
+    atomicAdd(&A.ev[4], n_examine);
+  }
+}
+
+}  // namespace
+}  // namespace fsig

@@ -5,11 +5,13 @@
 #include "../../include/fsig_gen.h"
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <memory>
 #include <thread>
+#include <unordered_map>
 #include <vector>
 
 namespace {
@@ -233,17 +235,32 @@ int fsig_gen_csr(uint32_t V, uint64_t E, const uint32_t* edges, uint32_t* offset
     adj[cur[a]++] = b;
     adj[cur[b]++] = a;
   }
+  // Sort and de-duplicate rows in parallel, then compact in one pass.
+  std::vector<uint32_t> uniq(V, 0);
+  const unsigned T = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+  std::vector<std::thread> th;
+  for (unsigned t = 0; t < T; t++) {
+    th.emplace_back([&, t] {
+      for (uint32_t v = t; v < V; v += T) {
+        uint32_t* row = adj + pos[v];
+        const size_t len = size_t(pos[v + 1] - pos[v]);
+        std::sort(row, row + len);
+        uint32_t u = 0, prev = 0xffffffffu;
+        for (size_t i = 0; i < len; i++) {
+          if (row[i] == prev) continue;
+          row[u++] = prev = row[i];
+        }
+        uniq[v] = u;
+      }
+    });
+  }
+  for (auto& x : th) x.join();
   uint64_t w = 0;
   offsets[0] = 0;
   for (uint32_t v = 0; v < V; v++) {
-    uint32_t* row = adj + pos[v];
-    size_t len = size_t(pos[v + 1] - pos[v]);
-    std::sort(row, row + len);
-    uint32_t prev = 0xffffffffu;
-    for (size_t i = 0; i < len; i++) {
-      if (row[i] == prev) continue;
-      adj[w++] = prev = row[i];
-    }
+    const uint32_t* row = adj + pos[v];
+    if (w != pos[v]) std::memmove(adj + w, row, sizeof(uint32_t) * uniq[v]);
+    w += uniq[v];
     offsets[v + 1] = uint32_t(w);
   }
   if (num_adj) *num_adj = w;
@@ -252,6 +269,12 @@ int fsig_gen_csr(uint32_t V, uint64_t E, const uint32_t* edges, uint32_t* offset
 
 int fsig_gen_query(uint32_t V, const uint32_t* off, const uint32_t* adj, const int32_t* labels, uint32_t n,
                    int mode, uint64_t seed, int32_t* qlabels, uint32_t* qedges, uint32_t* m, uint32_t* src) {
+  return fsig_gen_query_ex(V, off, adj, labels, n, mode, seed, INT32_MIN, qlabels, qedges, m, src);
+}
+
+int fsig_gen_query_ex(uint32_t V, const uint32_t* off, const uint32_t* adj, const int32_t* labels, uint32_t n,
+                      int mode, uint64_t seed, int32_t min_label, int32_t* qlabels, uint32_t* qedges, uint32_t* m,
+                      uint32_t* src) {
   if (n < 2 || n > 32 || !off || !adj || !labels || !qlabels || !qedges || !m || !src) return FSIG_GEN_EINVAL;
   if (mode != FSIG_QUERY_INDUCED && mode != FSIG_QUERY_DENSE && mode != FSIG_QUERY_SPARSE) return FSIG_GEN_EINVAL;
   Rng r(seed);
@@ -259,7 +282,7 @@ int fsig_gen_query(uint32_t V, const uint32_t* off, const uint32_t* adj, const i
   std::vector<std::pair<uint32_t, uint32_t>> walk_edges;
   for (int attempt = 0; attempt < 4000; attempt++) {
     uint32_t start = r.below(V);
-    if (off[start + 1] == off[start]) continue;
+    if (off[start + 1] == off[start] || labels[start] < min_label) continue;
     set.assign(1, start);
     walk_edges.clear();
     uint32_t cur = start;
@@ -268,11 +291,72 @@ int fsig_gen_query(uint32_t V, const uint32_t* off, const uint32_t* adj, const i
         if (set[i] == v) return int(i);
       return -1;
     };
+    if (mode == FSIG_QUERY_DENSE) {
+      // Randomised greedy walk: with probability 3/4 step to a frontier
+      // vertex with the most edges into the set (ties at random), otherwise
+      // to a uniformly random frontier vertex.  Frontier edge counts are
+      // kept incrementally as vertices join.
+      std::vector<std::pair<uint32_t, uint32_t>> front;  // (vertex, edges into set), by first appearance
+      std::unordered_map<uint32_t, uint32_t> where;       // vertex -> index in front
+      auto add = [&](uint32_t v) {
+        for (uint32_t k = off[v]; k < off[v + 1]; k++) {
+          const uint32_t c = adj[k];
+          if (labels[c] < min_label) continue;
+          auto it = where.find(c);
+          if (it == where.end()) {
+            where.emplace(c, uint32_t(front.size()));
+            front.emplace_back(c, 1u);
+          } else if (front[it->second].second != 0xffffffffu) {
+            front[it->second].second++;
+          }
+        }
+        auto it = where.find(v);
+        if (it == where.end()) {
+          where.emplace(v, uint32_t(front.size()));
+          front.emplace_back(v, 0xffffffffu);
+        } else {
+          front[it->second].second = 0xffffffffu;  // in the set
+        }
+      };
+      add(start);
+      while (set.size() < n) {
+        uint32_t pick = 0xffffffffu;
+        if ((r.next() & 3) != 0) {
+          uint32_t best = 0, ties = 0;
+          for (auto& fc : front) {
+            if (fc.second == 0xffffffffu) continue;
+            if (fc.second > best) { best = fc.second; ties = 1; pick = fc.first; }
+            else if (fc.second == best && r.below(++ties) == 0) pick = fc.first;
+          }
+        } else {
+          uint32_t live = 0;
+          for (auto& fc : front) live += fc.second != 0xffffffffu;
+          if (live) {
+            uint32_t k = r.below(live);
+            for (auto& fc : front) {
+              if (fc.second == 0xffffffffu) continue;
+              if (k-- == 0) { pick = fc.first; break; }
+            }
+          }
+        }
+        if (pick == 0xffffffffu) break;
+        set.push_back(pick);
+        add(pick);
+      }
+    }
     for (uint32_t step = 0; step < 64 * n && set.size() < n; step++) {
-      if (mode == FSIG_QUERY_DENSE && set.size() > 1 && (r.next() & 1)) cur = set[r.below(uint32_t(set.size()))];
       uint32_t d = off[cur + 1] - off[cur];
       if (d == 0) break;
       uint32_t nxt = adj[off[cur] + r.below(d)];
+      if (labels[nxt] < min_label) {
+        // resample among the qualifying neighbours (bounded tries)
+        bool found = false;
+        for (int t = 0; t < 32 && !found; t++) {
+          nxt = adj[off[cur] + r.below(d)];
+          found = labels[nxt] >= min_label;
+        }
+        if (!found) continue;
+      }
       int ci = index_of(cur), ni = index_of(nxt);
       if (ni < 0) { set.push_back(nxt); ni = int(set.size()) - 1; }
       uint32_t a = uint32_t(ci), b = uint32_t(ni);
@@ -294,7 +378,10 @@ int fsig_gen_query(uint32_t V, const uint32_t* off, const uint32_t* adj, const i
     }
     std::sort(es.begin(), es.end());
     es.erase(std::unique(es.begin(), es.end()), es.end());
-    if (mode == FSIG_QUERY_DENSE && !(2 * es.size() > 3 * size_t(n))) continue;
+    // dense: average degree above 3, or above 0.75 (n - 1) where 3 is out of
+    // reach (n = 4 has at most average degree 3)
+    if (mode == FSIG_QUERY_DENSE && !(8 * es.size() > std::min<size_t>(12 * size_t(n), 3 * size_t(n) * (n - 1))))
+      continue;
     if (mode == FSIG_QUERY_SPARSE && !(2 * es.size() <= 3 * size_t(n))) continue;
     for (uint32_t i = 0; i < n; i++) {
       src[i] = set[i];

@@ -288,7 +288,11 @@ __global__ void signature_from_rows_kernel(const int32_t* __restrict__ label, co
   }
 }
 
-__global__ void narrow_check_kernel(const uint32_t* total, uint32_t* dst) { *dst = *total; }
+__global__ void gather_kernel(const uint32_t* __restrict__ idx, uint64_t n, const uint32_t* __restrict__ table,
+                              uint32_t* out) {
+  for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x)
+    out[i] = table[idx[i]];
+}
 
 inline unsigned grid_for(uint64_t n, int threads, int sms) {
   uint64_t b = (n + threads - 1) / threads;
@@ -442,7 +446,12 @@ int build_device_graph(Engine& e, uint32_t V, const int32_t* h_labels, uint64_t 
   g.base = e.arena.take<uint32_t>(uint64_t(L) + 1);
   g.lseg = e.arena.take<uint32_t>(uint64_t(V) * (uint64_t(L) + 1));
   g.sig = e.arena.take<uint4>(uint64_t(V) * 4);
-  if (!g.base || !g.lseg || !g.sig) return fail(FSIG_EADMISSION, "graph tables do not fit the device arena");
+  g.adj_old = e.arena.take<uint32_t>(std::max<uint64_t>(g.nadj, 1));
+  if (!g.base || !g.lseg || !g.sig || !g.adj_old) return fail(FSIG_EADMISSION, "graph tables do not fit the device arena");
+  if (g.nadj) {
+    gather_kernel<<<grid_for(g.nadj, 256, e.num_sms), 256, 0, s>>>(g.adj, g.nadj, g.old_of_new, g.adj_old);
+    FSIG_CUDA_TRY(cudaGetLastError());
+  }
   FSIG_CUDA_TRY(cudaMemcpyAsync(g.base, g.h_base.data(), sizeof(uint32_t) * (L + 1), cudaMemcpyHostToDevice, s));
   label_segments_kernel<<<grid_for(uint64_t(V) * (L + 1), 256, e.num_sms), 256, 0, s>>>(g.off, g.adj, g.base, V, L,
                                                                                        g.lseg);

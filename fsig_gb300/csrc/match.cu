@@ -27,6 +27,7 @@ struct GraphView {
   const uint32_t* __restrict__ lseg;
   const uint4* __restrict__ sig;
   const uint32_t* __restrict__ old_of_new;
+  const uint32_t* __restrict__ adj_old;
 };
 
 namespace {
@@ -35,7 +36,7 @@ constexpr uint32_t kFull = 0xffffffffu;
 constexpr int kChunk = 32;  // driver elements examined per refill (one per lane)
 
 GraphView view_of(const DeviceGraph& g) {
-  return GraphView{g.V, g.L, g.label, g.off, g.adj, g.lseg, g.sig, g.old_of_new};
+  return GraphView{g.V, g.L, g.label, g.off, g.adj, g.lseg, g.sig, g.old_of_new, g.adj_old};
 }
 
 // ---------------------------------------------------------------------------
@@ -297,7 +298,8 @@ __global__ void order_kernel(const QVert* __restrict__ qv, const uint32_t* __res
 // Roots of each query in ascending vertex order (block scan of word popcounts).
 __global__ void __launch_bounds__(256) roots_kernel(const QVert* __restrict__ qv, const Plan* __restrict__ plans,
                                                     uint32_t Q, const uint32_t* __restrict__ root_off,
-                                                    const uint32_t* __restrict__ pool, uint32_t* roots) {
+                                                    const uint32_t* __restrict__ pool, uint32_t* roots,
+                                                    uint32_t* root_q) {
   __shared__ uint32_t sw[33];
   for (uint32_t q = blockIdx.x; q < Q; q += gridDim.x) {
     const Plan* p = plans + q;
@@ -314,6 +316,7 @@ __global__ void __launch_bounds__(256) roots_kernel(const QVert* __restrict__ qv
       while (wbits) {
         const uint32_t bit = __ffs(wbits) - 1;
         wbits &= wbits - 1;
+        root_q[k] = q;
         roots[k++] = r->bmbase + (i << 5) + bit;
       }
       outp += total;
@@ -321,228 +324,32 @@ __global__ void __launch_bounds__(256) roots_kernel(const QVert* __restrict__ qv
   }
 }
 
-// ---------------------------------------------------------------------------
-// Enumeration: a persistent grid; each warp repeatedly takes `chunk` root
-// tasks from a global counter and runs a depth-first extension of each root.
-//
-// Level state lives in registers distributed over lanes: lane j holds, for
-// depth j, the mapped vertex f_j, the partial hash S_j, the driver cursor
-// (dpos_j, dend_j, drv_j) and the candidate buffer cursor (cnt_j, it_j).  The
-// candidate buffers (32 per depth) and the plan live in shared memory.
-//
-// Candidates at depth i are the driver list (the shortest label-l(i) segment
-// among the backward neighbours' rows), examined 32 at a time, one per lane:
-// injectivity against same-label earlier positions, the candidate bitmap of
-// position i, then a binary search in every other backward segment.
-// ---------------------------------------------------------------------------
-struct WarpSmem {
-  Plan plan;
-  uint32_t cand[kMaxQ][kChunk];
-};
-
-__device__ __forceinline__ bool contains(const uint32_t* __restrict__ a, uint32_t lo, uint32_t hi, uint32_t x,
-                                         unsigned long long& bytes) {
-  while (lo < hi) {
-    const uint32_t mid = (lo + hi) >> 1;
-    const uint32_t y = __ldg(a + mid);
-    bytes += 4;
-    if (y < x) lo = mid + 1;
-    else if (y > x) hi = mid;
-    else return true;
-  }
-  return false;
-}
-
-__global__ void __launch_bounds__(256) enumerate_kernel(GraphView g, const Plan* __restrict__ plans,
-                                                        const uint32_t* __restrict__ pool,
-                                                        const uint32_t* __restrict__ roots,
-                                                        const uint32_t* __restrict__ root_off, uint32_t Q,
-                                                        uint32_t chunk, uint32_t* task_next, QueryResult* res,
-                                                        unsigned long long* algo_bytes, unsigned long long seed) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  WarpSmem& ws = reinterpret_cast<WarpSmem*>(smem_raw)[threadIdx.x >> 5];
-  const uint32_t lane = threadIdx.x & 31;
-  const uint32_t T = root_off[Q];
+// Number of pass-0 tasks per root: its depth-1 driver range in chunks of
+// `split` entries (at least one task per root, so every root is counted).
+__global__ void root_chunks_kernel(GraphView g, const Plan* __restrict__ plans, const uint32_t* __restrict__ roots,
+                                   const uint32_t* __restrict__ root_q, const uint32_t* __restrict__ total_roots,
+                                   uint32_t split, uint32_t* chunks) {
+  const uint32_t nr = *total_roots;
   const uint64_t W1 = uint64_t(g.L) + 1;
-
-  // lane-distributed level state
-  uint32_t f = 0, dpos = 0, dend = 0, drv = 0, cnt = 0, it = 0;
-  unsigned long long S = 0, lc = 0;
-  unsigned long long my_count = 0, my_hash = 0, bytes = 0;
-  uint32_t cur_q = kInvalid;
-
-  auto flush = [&](uint32_t q) {
-    if (q == kInvalid) return;
-    unsigned long long c = warp_sum(my_count), h = warp_sum(my_hash);
-    if (lane == 0) {
-      atomicAdd(&res[q].count, c);
-      atomicAdd(&res[q].hash, h);
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nr; i += gridDim.x * blockDim.x) {
+    const Plan* p = plans + root_q[i];
+    uint32_t c = 1;
+    if (p->n > 1) {
+      const uint32_t* s = g.lseg + uint64_t(roots[i]) * W1 + p->lab[1];
+      const uint32_t len = s[1] - s[0];
+      c = max(1u, (len + split - 1) / split);
     }
-    if (lane < ws.plan.n && lc) atomicAdd(&res[q].levels[lane], lc);
-    my_count = my_hash = 0;
-    lc = 0;
-  };
-
-  // Computes the driver of depth `lv` from the mapped vertices of its
-  // backward neighbours; stores it in lane lv's registers.
-  auto enter = [&](uint32_t lv) {
-    const uint32_t bw = ws.plan.bwd[lv];
-    const int32_t lab = ws.plan.lab[lv];
-    uint32_t lo = 0, hi = 0, len = kInvalid;
-    if ((bw >> lane) & 1u) {
-      const uint32_t* s = g.lseg + uint64_t(f) * W1 + lab;
-      lo = s[0];
-      hi = s[1];
-      len = hi - lo;
-      bytes += 8;
-    }
-    const bool empty = __ballot_sync(kFull, len == 0) != 0;
-    const uint32_t j = warp_argmin(float(len), len == kInvalid ? 0xffffu : lane);
-    const uint32_t dlo = __shfl_sync(kFull, lo, j & 31), dhi = __shfl_sync(kFull, hi, j & 31);
-    if (lane == lv) {
-      dpos = dlo;
-      dend = empty ? dlo : dhi;
-      drv = j;
-      cnt = 0;
-      it = 0;
-    }
-  };
-
-  // Examines the next 32 driver entries of depth lv; returns the candidate
-  // predicate and the candidate (one per lane).
-  auto examine = [&](uint32_t lv, uint32_t& x) -> bool {
-    const uint32_t dp = __shfl_sync(kFull, dpos, lv), de = __shfl_sync(kFull, dend, lv);
-    const uint32_t dv = __shfl_sync(kFull, drv, lv);
-    const int32_t lab = ws.plan.lab[lv];
-    uint32_t bw = ws.plan.bwd[lv] & ~(1u << dv);
-    uint32_t my_lo = 0, my_hi = 0;
-    if ((bw >> lane) & 1u) {
-      const uint32_t* s = g.lseg + uint64_t(f) * W1 + lab;
-      my_lo = s[0];
-      my_hi = s[1];
-      bytes += 8;
-    }
-    const uint32_t k = dp + lane;
-    bool pred = k < de;
-    x = pred ? __ldg(g.adj + k) : 0u;
-    if (pred) bytes += 4;
-    uint32_t sm = ws.plan.same[lv];
-    while (sm) {
-      const uint32_t j = __ffs(sm) - 1;
-      sm &= sm - 1;
-      const uint32_t fj = __shfl_sync(kFull, f, j);
-      pred = pred && x != fj;
-    }
-    if (pred) {
-      const uint32_t bit = x - ws.plan.bmbase[lv];
-      pred = (__ldg(pool + ws.plan.bmoff[lv] + (bit >> 5)) >> (bit & 31)) & 1u;
-      bytes += 4;
-    }
-    while (bw) {
-      const uint32_t j = __ffs(bw) - 1;
-      bw &= bw - 1;
-      const uint32_t lo = __shfl_sync(kFull, my_lo, j), hi = __shfl_sync(kFull, my_hi, j);
-      if (pred) pred = contains(g.adj, lo, hi, x, bytes);
-    }
-    if (lane == lv) dpos = dp + kChunk;
-    return pred;
-  };
-
-  for (;;) {
-    uint32_t t0 = 0;
-    if (lane == 0) t0 = atomicAdd(task_next, chunk);
-    t0 = __shfl_sync(kFull, t0, 0);
-    if (t0 >= T) break;
-    const uint32_t t1 = min(t0 + chunk, T);
-    for (uint32_t t = t0; t < t1; t++) {
-      if (cur_q == kInvalid || t < root_off[cur_q] || t >= root_off[cur_q + 1]) {
-        uint32_t lo = 0, hi = Q;  // last q with root_off[q] <= t
-        while (hi - lo > 1) {
-          const uint32_t mid = (lo + hi) >> 1;
-          if (root_off[mid] <= t) lo = mid; else hi = mid;
-        }
-        while (lo + 1 < Q && root_off[lo + 1] <= t) lo++;
-        flush(cur_q);
-        __syncwarp();
-        const uint32_t* src = reinterpret_cast<const uint32_t*>(plans + lo);
-        uint32_t* dstp = reinterpret_cast<uint32_t*>(&ws.plan);
-        for (uint32_t i = lane; i < sizeof(Plan) / 4; i += 32) dstp[i] = src[i];
-        __syncwarp();
-        cur_q = lo;
-      }
-      const uint32_t n = ws.plan.n;
-      const uint32_t r = roots[t];
-      const unsigned long long S0 = fmix64((uint64_t(ws.plan.qv[0]) << 32) | g.old_of_new[r]);
-      if (lane == 0) {
-        f = r;
-        S = S0;
-        lc += 1;
-      }
-      if (n == 1) {
-        if (lane == 0) {
-          my_count += 1;
-          my_hash += fmix64(seed + S0);
-        }
-        continue;
-      }
-      uint32_t lv = 1;
-      enter(1);
-      while (true) {
-        if (lv == n - 1) {
-          // leaf depth: count and hash every surviving candidate
-          const unsigned long long Sp = __shfl_sync(kFull, S, lv - 1);
-          const uint64_t tb = uint64_t(ws.plan.qv[lv]) << 32;
-          while (__shfl_sync(kFull, dpos, lv) < __shfl_sync(kFull, dend, lv)) {
-            uint32_t x;
-            const bool p = examine(lv, x);
-            const uint32_t m = __ballot_sync(kFull, p);
-            if (p) {
-              my_count += 1;
-              my_hash += fmix64(seed + Sp + fmix64(tb | __ldg(g.old_of_new + x)));
-              bytes += 4;
-            }
-            if (lane == lv) lc += __popc(m);
-          }
-          lv--;
-          if (lv == 0) break;
-          continue;
-        }
-        const uint32_t i = __shfl_sync(kFull, it, lv), c = __shfl_sync(kFull, cnt, lv);
-        if (i < c) {
-          const uint32_t x = ws.cand[lv][i];
-          const unsigned long long Sp = __shfl_sync(kFull, S, lv - 1);
-          if (lane == lv) {
-            it = i + 1;
-            f = x;
-            S = Sp + fmix64((uint64_t(ws.plan.qv[lv]) << 32) | __ldg(g.old_of_new + x));
-            bytes += 4;
-          }
-          lv++;
-          enter(lv);
-          continue;
-        }
-        if (__shfl_sync(kFull, dpos, lv) < __shfl_sync(kFull, dend, lv)) {
-          uint32_t x;
-          const bool p = examine(lv, x);
-          const uint32_t m = __ballot_sync(kFull, p);
-          if (p) ws.cand[lv][__popc(m & lanemask_lt())] = x;
-          __syncwarp();
-          if (lane == lv) {
-            cnt = __popc(m);
-            it = 0;
-            lc += __popc(m);
-          }
-          continue;
-        }
-        lv--;
-        if (lv == 0) break;
-      }
-    }
+    chunks[i] = c;
   }
-  flush(cur_q);
-  bytes = warp_sum(bytes);
-  if (lane == 0) atomicAdd(algo_bytes, bytes);
 }
+
+}  // namespace
+}  // namespace fsig
+
+#include "enumerate.cuh"
+
+namespace fsig {
+namespace {
 
 inline unsigned grid_cap(uint64_t n, int threads, int sms, int per_sm) {
   uint64_t b = (n + threads - 1) / threads;
@@ -688,13 +495,16 @@ T* upload(Engine& e, const std::vector<T>& v, int& rc) {
   if (!v.empty()) {
     cudaError_t err = cudaMemcpyAsync(d, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, e.stream);
     if (err != cudaSuccess) { rc = fail_cuda(err, "cudaMemcpyAsync", __FILE__, __LINE__); return nullptr; }
+    e.cur_h2d += sizeof(T) * v.size();
   }
   return d;
 }
 
 // Filter + refine + popcount on the device.  Returns the final pool.
 int filter_stage(Engine& e, const BatchLayout& b, uint32_t mode, int refine_iters, QVert* d_qv, uint64_t* d_gword,
-                 uint32_t* d_lab_gidx, uint32_t* d_lab_begin, uint32_t*& pool, uint32_t* d_counts) {
+                 uint32_t* d_lab_gidx, uint32_t* d_lab_begin, uint32_t*& pool, uint32_t* d_counts,
+                 uint32_t* launches = nullptr) {
+  uint32_t nl = 1;
   const DeviceGraph& g = e.g;
   cudaStream_t s = e.stream;
   uint32_t* p0 = e.arena.take<uint32_t>(std::max<uint64_t>(b.words, 1));
@@ -711,12 +521,111 @@ int filter_stage(Engine& e, const BatchLayout& b, uint32_t mode, int refine_iter
     refine_kernel<<<grid_cap(runs * 32, 256, e.num_sms, 16), 256, 0, s>>>(gv, d_qv, b.G, d_gword, b.words, cur, nxt);
     FSIG_CUDA_TRY(cudaGetLastError());
     std::swap(cur, nxt);
+    nl++;
   }
   if (b.G) {
     popcount_kernel<<<std::min<uint32_t>(b.G, e.num_sms * 8), 256, 0, s>>>(d_qv, b.G, cur, d_counts);
     FSIG_CUDA_TRY(cudaGetLastError());
+    nl++;
   }
+  if (launches) *launches += nl;
   pool = cur;
+  return FSIG_OK;
+}
+}  // namespace
+
+namespace {
+constexpr uint32_t kOverflowCap = 1u << 20;  // task records per overflow queue
+
+// Runs the enumeration kernel over pass-0 tasks, then over the records each
+// pass leaves in its overflow queue, until none are left.
+int enumerate_passes(Engine& e, const BatchOptions& opt, const GraphView& gv, const Plan* d_plans,
+                     const uint32_t* pool, uint32_t Q, const uint32_t* d_roots, const uint32_t* d_root_q,
+                     const uint32_t* d_chunk_off, uint32_t nroots, uint32_t split, QueryResult* d_res,
+                     unsigned long long* d_misc, uint32_t& passes, float& ms_enum, uint64_t& d2h) {
+  cudaStream_t s = e.stream;
+  TaskRec* qa = e.arena.take<TaskRec>(kOverflowCap);
+  TaskRec* qb = e.arena.take<TaskRec>(kOverflowCap);
+  uint32_t* ra = e.arena.take<uint32_t>(kOverflowCap);
+  uint32_t* rb = e.arena.take<uint32_t>(kOverflowCap);
+  uint32_t* ctr = e.arena.take<uint32_t>(8 * kCtrStride);
+  if (!qa || !qb || !ra || !rb || !ctr) return fail(FSIG_EADMISSION, "work queues do not fit the device arena");
+  FSIG_CUDA_TRY(cudaMemsetAsync(ra, 0, sizeof(uint32_t) * kOverflowCap, s));
+  FSIG_CUDA_TRY(cudaMemsetAsync(rb, 0, sizeof(uint32_t) * kOverflowCap, s));
+  const uint32_t wpb = std::max<uint32_t>(1, std::min<uint32_t>(opt.warps_per_block, 8));
+  const size_t smem = sizeof(WarpSmem) * wpb;
+  if (e.enum_per_sm == 0) {
+    FSIG_CUDA_TRY(cudaFuncSetAttribute(enumerate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       int(sizeof(WarpSmem) * 8)));
+    int per = 0;
+    FSIG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, enumerate_kernel, 8 * 32,
+                                                                sizeof(WarpSmem) * 8));
+    e.enum_per_sm = std::max(per, 1);
+  }
+  const int per_sm = wpb == 8 ? e.enum_per_sm : std::max(1, e.enum_per_sm * 8 / int(wpb));
+  EnumArgs A;
+  A.g = gv;
+  A.plans = d_plans;
+  A.pool = pool;
+  A.Q = Q;
+  A.roots = d_roots;
+  A.root_q = d_root_q;
+  A.chunk_off = d_chunk_off;
+  A.nroots = nroots;
+  A.split = split;
+  A.in_tasks = nullptr;
+  A.in_count = 0;
+  A.out_cap = kOverflowCap;
+  A.ctr = ctr;
+  A.chunk = std::max<uint32_t>(opt.chunk, 1);
+  A.res = d_res;
+  A.work_cap = opt.max_work;
+  A.algo_bytes = d_misc + 1;
+  unsigned long long* d_ev = e.arena.take<unsigned long long>(8);
+  if (!d_ev) return fail(FSIG_EADMISSION, "arena");
+  FSIG_CUDA_TRY(cudaMemsetAsync(d_ev, 0, 64, s));
+  A.ev = d_ev;
+  A.seed = FSIG_HASH_SEED;
+  TaskRec* out = qa;
+  uint32_t* ready = ra;
+  TaskRec* other = qb;
+  uint32_t* other_ready = rb;
+  passes = 0;
+  FSIG_CUDA_TRY(cudaMemsetAsync(d_misc + 1, 0, sizeof(unsigned long long), s));
+  for (uint32_t pass = 0;; pass++) {
+    A.out_tasks = out;
+    A.out_ready = ready;
+    A.tag = pass + 1;
+    A.budget = (long long)opt.budget_cycles;
+    // every warp starts active; idle warps are counted as they wait
+    uint32_t init[8 * kCtrStride] = {0};
+    init[5 * kCtrStride] = uint32_t(e.num_sms * per_sm) * wpb;
+    FSIG_CUDA_TRY(cudaMemcpyAsync(ctr, init, sizeof(init), cudaMemcpyHostToDevice, s));
+    FSIG_CUDA_TRY(cudaEventRecord(e.ev_enum[0], s));
+    enumerate_kernel<<<e.num_sms * per_sm, wpb * 32, smem, s>>>(A);
+    FSIG_CUDA_TRY(cudaGetLastError());
+    FSIG_CUDA_TRY(cudaEventRecord(e.ev_enum[1], s));
+    passes++;
+    uint32_t hc[4 * kCtrStride];
+    FSIG_CUDA_TRY(cudaMemcpyAsync(hc, ctr, sizeof(hc), cudaMemcpyDeviceToHost, s));
+    FSIG_CUDA_TRY(cudaStreamSynchronize(s));
+    float ms = 0;
+    FSIG_CUDA_TRY(cudaEventElapsedTime(&ms, e.ev_enum[0], e.ev_enum[1]));
+    ms_enum += ms;
+    d2h += sizeof(hc);
+    const uint32_t h[4] = {hc[0], hc[kCtrStride], hc[2 * kCtrStride], hc[3 * kCtrStride]};
+    if (h[3] & kErrTimeout) return fail(FSIG_ETIMEOUT, "a work-queue record was not published in time");
+    const uint32_t head = h[2], tail = std::min(h[1], kOverflowCap);
+    if (head >= tail) break;
+    // unconsumed records become the next pass's input
+    A.in_tasks = out + head;
+    A.in_count = tail - head;
+    std::swap(out, other);
+    std::swap(ready, other_ready);
+    if (pass > 4096) return fail(FSIG_EOVERFLOW, "enumeration did not converge");
+  }
+  FSIG_CUDA_TRY(cudaMemcpyAsync(e.last_ev, d_ev, sizeof(e.last_ev), cudaMemcpyDeviceToHost, s));
+  FSIG_CUDA_TRY(cudaStreamSynchronize(s));
   return FSIG_OK;
 }
 }  // namespace
@@ -735,6 +644,9 @@ int run_batch(Engine& e, const std::vector<HostQuery>& qs, const BatchOptions& o
   if (Q == 0) return FSIG_OK;
   if (b.root_cap > 0xffffffffull) return fail(FSIG_EADMISSION, "batch has more than 2^32 root candidates");
   e.arena.release(g.arena_mark);
+  e.cur_h2d = 0;
+  uint64_t d2h = 0;
+  uint32_t launches = 0;
   int rc = FSIG_OK;
   QVert* d_qv = upload(e, b.qv, rc);
   if (rc) return rc;
@@ -763,13 +675,14 @@ int run_batch(Engine& e, const std::vector<HostQuery>& qs, const BatchOptions& o
   uint32_t* d_rootoff = e.arena.take<uint32_t>(uint64_t(Q) + 1);
   uint32_t* d_orders = e.arena.take<uint32_t>(uint64_t(Q) * kMaxQ);
   QueryResult* d_res = e.arena.take<QueryResult>(Q);
-  unsigned long long* d_misc = e.arena.take<unsigned long long>(4);  // [0] task_next, [1] algo bytes
+  unsigned long long* d_misc = e.arena.take<unsigned long long>(4);  // [1] modelled bytes
   if (!d_counts || !d_plans || !d_rootcnt || !d_rootoff || !d_orders || !d_res || !d_misc)
     return fail(FSIG_EADMISSION, "batch does not fit the device arena");
 
   FSIG_CUDA_TRY(cudaEventRecord(e.ev[0], s));
   uint32_t* pool = nullptr;
-  rc = filter_stage(e, b, opt.filter_mode, opt.refine_iters, d_qv, d_gword, d_lab_gidx, d_lab_begin, pool, d_counts);
+  rc = filter_stage(e, b, opt.filter_mode, opt.refine_iters, d_qv, d_gword, d_lab_gidx, d_lab_begin, pool, d_counts,
+                    &launches);
   if (rc) return rc;
   FSIG_CUDA_TRY(cudaEventRecord(e.ev[1], s));
 
@@ -778,6 +691,7 @@ int run_batch(Engine& e, const std::vector<HostQuery>& qs, const BatchOptions& o
     // Reference-exact orders are computed on the host from the counts.
     FSIG_CUDA_TRY(cudaMemcpyAsync(out.counts.data(), d_counts, sizeof(uint32_t) * b.G, cudaMemcpyDeviceToHost, s));
     FSIG_CUDA_TRY(cudaStreamSynchronize(s));
+    d2h += sizeof(uint32_t) * b.G;
     for (uint32_t q = 0; q < Q; q++) {
       bool any_zero = false;
       for (uint32_t u = 0; u < qs[q].n; u++) any_zero |= out.counts[b.qoff[q] + u] == 0;
@@ -793,30 +707,45 @@ int run_batch(Engine& e, const std::vector<HostQuery>& qs, const BatchOptions& o
       opt.host_order(qs[q], out.counts.data() + b.qoff[q], given.data() + b.qoff[q]);
     }
     FSIG_CUDA_TRY(cudaMemcpyAsync(d_given, given.data(), sizeof(uint32_t) * b.G, cudaMemcpyHostToDevice, s));
+    e.cur_h2d += sizeof(uint32_t) * b.G;
     order_mode = kOrderGiven;
   }
   uint32_t* d_roots = e.arena.take<uint32_t>(std::max<uint64_t>(b.root_cap, 1));
-  if (!d_roots) return fail(FSIG_EADMISSION, "root list does not fit the device arena");
+  uint32_t* d_root_q = e.arena.take<uint32_t>(std::max<uint64_t>(b.root_cap, 1));
+  uint32_t* d_chunks = e.arena.take<uint32_t>(std::max<uint64_t>(b.root_cap, 1) + 1);
+  uint32_t* d_chunk_off = e.arena.take<uint32_t>(std::max<uint64_t>(b.root_cap, 1) + 1);
+  if (!d_roots || !d_root_q || !d_chunks || !d_chunk_off)
+    return fail(FSIG_EADMISSION, "root list does not fit the device arena");
   FSIG_CUDA_TRY(cudaMemsetAsync(d_rootcnt, 0, sizeof(uint32_t) * (uint64_t(Q) + 1), s));
   order_kernel<<<(Q + 7) / 8, 256, 0, s>>>(d_qv, d_qoff, Q, d_counts, order_mode, d_scores, d_given, d_plans,
                                            d_rootcnt, d_orders);
   FSIG_CUDA_TRY(cudaGetLastError());
-  rc = device_exclusive_scan<uint32_t>(e.arena, d_rootcnt, d_rootoff, uint64_t(Q) + 1, nullptr, s);
+  rc = device_exclusive_scan<uint32_t>(e.arena, d_rootcnt, d_rootoff, uint64_t(Q) + 1, nullptr, s, &launches);
   if (rc) return rc;
-  roots_kernel<<<std::min<uint32_t>(Q, e.num_sms * 8), 256, 0, s>>>(d_qv, d_plans, Q, d_rootoff, pool, d_roots);
+  roots_kernel<<<std::min<uint32_t>(Q, e.num_sms * 8), 256, 0, s>>>(d_qv, d_plans, Q, d_rootoff, pool, d_roots,
+                                                                     d_root_q);
   FSIG_CUDA_TRY(cudaGetLastError());
+  launches += 2;
+  // pass-0 task space: depth-1 chunks of every root
+  uint32_t nroots = 0;
+  FSIG_CUDA_TRY(cudaMemcpyAsync(&nroots, d_rootoff + Q, 4, cudaMemcpyDeviceToHost, s));
+  FSIG_CUDA_TRY(cudaStreamSynchronize(s));
+  d2h += 4;
+  const uint32_t split = std::max<uint32_t>(opt.split, 32);
+  FSIG_CUDA_TRY(cudaMemsetAsync(d_chunks, 0, sizeof(uint32_t) * (uint64_t(nroots) + 1), s));
+  if (nroots) {
+    root_chunks_kernel<<<grid_cap(nroots, 256, e.num_sms, 8), 256, 0, s>>>(view_of(g), d_plans, d_roots, d_root_q,
+                                                                          d_rootoff + Q, split, d_chunks);
+    FSIG_CUDA_TRY(cudaGetLastError());
+    launches++;
+  }
+  rc = device_exclusive_scan<uint32_t>(e.arena, d_chunks, d_chunk_off, uint64_t(nroots) + 1, nullptr, s, &launches);
+  if (rc) return rc;
   FSIG_CUDA_TRY(cudaMemsetAsync(d_res, 0, sizeof(QueryResult) * Q, s));
-  FSIG_CUDA_TRY(cudaMemsetAsync(d_misc, 0, sizeof(unsigned long long) * 4, s));
-  const uint32_t wpb = std::max<uint32_t>(1, std::min<uint32_t>(opt.warps_per_block, 8));
-  const size_t smem = sizeof(WarpSmem) * wpb;
-  FSIG_CUDA_TRY(cudaFuncSetAttribute(enumerate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-  int per_sm = 0;
-  FSIG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, enumerate_kernel, int(wpb * 32), smem));
-  per_sm = std::max(per_sm, 1);
-  enumerate_kernel<<<e.num_sms * per_sm, wpb * 32, smem, s>>>(
-      view_of(g), d_plans, pool, d_roots, d_rootoff, Q, std::max<uint32_t>(opt.chunk, 1),
-      reinterpret_cast<uint32_t*>(d_misc), d_res, d_misc + 1, FSIG_HASH_SEED);
-  FSIG_CUDA_TRY(cudaGetLastError());
+  rc = enumerate_passes(e, opt, view_of(g), d_plans, pool, Q, d_roots, d_root_q, d_chunk_off, nroots, split, d_res,
+                        d_misc, out.passes, out.ms_enum, d2h);
+  if (rc) return rc;
+  launches += out.passes;
   FSIG_CUDA_TRY(cudaEventRecord(e.ev[2], s));
 
   FSIG_CUDA_TRY(cudaMemcpyAsync(out.res.data(), d_res, sizeof(QueryResult) * Q, cudaMemcpyDeviceToHost, s));
@@ -829,6 +758,24 @@ int run_batch(Engine& e, const std::vector<HostQuery>& qs, const BatchOptions& o
   for (uint32_t q = 0; q < Q; q++) out.ok[q] = hp[q].ok;
   FSIG_CUDA_TRY(cudaEventElapsedTime(&out.ms_filter, e.ev[0], e.ev[1]));
   FSIG_CUDA_TRY(cudaEventElapsedTime(&out.ms_join, e.ev[1], e.ev[2]));
+  d2h += sizeof(QueryResult) * Q + sizeof(uint32_t) * b.G + sizeof(uint32_t) * Q * kMaxQ +
+         sizeof(unsigned long long) + sizeof(Plan) * Q;
+  out.h2d_bytes = e.cur_h2d;
+  out.d2h_bytes = d2h;
+  out.launches = launches;
+  e.last.h2d_bytes = out.h2d_bytes;
+  e.last.d2h_bytes = out.d2h_bytes;
+  e.last.enum_bytes = out.algo_bytes;
+  e.last.kernel_launches = out.launches;
+  e.last.enum_passes = out.passes;
+  e.last.ms_filter = out.ms_filter;
+  e.last.ms_join = out.ms_join;
+  e.last.ms_enum = out.ms_enum;
+  e.last.enum_tasks = e.last_ev[0];
+  e.last.enum_pops = e.last_ev[1];
+  e.last.enum_handoffs = e.last_ev[2];
+  e.last.enum_records = e.last_ev[3];
+  e.last.enum_examines = e.last_ev[4];
   e.arena.release(g.arena_mark);
   return FSIG_OK;
 }

@@ -71,13 +71,19 @@ struct QueryResult {
   unsigned long long count;
   unsigned long long hash;
   unsigned long long levels[kMaxQ];
+  unsigned long long work;   // driver entries examined so far (with a limit)
+  unsigned int aborted;      // 1: the limit was exceeded
+  unsigned int pad;
 };
 
 struct BatchOptions {
   uint32_t filter_mode = kFilterDegree | kFilterSignature;
   int refine_iters = 0;
   uint32_t order_mode = kOrderGSI;
-  uint32_t chunk = 4;        // root tasks per grab
+  uint32_t chunk = 4;        // tasks per grab
+  uint32_t split = 256;      // driver entries per task range
+  long long budget_cycles = 4000;     // cycles on a task before it may be split for idle warps
+  unsigned long long max_work = 0;  // per-query limit on examined driver entries (0: none)
   uint32_t warps_per_block = 8;
   const float* scores = nullptr;  // host scores per query vertex (kOrderScores), batch order
   // When set, candidate counts are brought to the host after filtering and
@@ -91,7 +97,11 @@ struct BatchOutput {
   std::vector<uint32_t> orders;    // kMaxQ per query
   std::vector<uint32_t> ok;
   float ms_filter = 0, ms_join = 0;
-  unsigned long long algo_bytes = 0;  // modelled bytes read by the enumerator
+  unsigned long long algo_bytes = 0;  // bytes the enumerator's loads request
+  uint32_t passes = 0;                // enumeration passes run
+  uint64_t h2d_bytes = 0, d2h_bytes = 0;
+  uint32_t launches = 0;
+  float ms_enum = 0;
 };
 
 // Runs filter -> refine -> order -> roots -> enumerate for a batch.
@@ -103,5 +113,6 @@ int run_filter_probe(Engine& e, const HostQuery& q, uint32_t filter_mode, int re
 // Host-side reference orders (plan.cpp).
 void gsi_order_host(const HostQuery& q, const uint32_t* cand, uint32_t* order);
 void mmatch_order_host(const HostQuery& q, const uint32_t* cand, uint32_t* order);
+void mmatch_structure(const HostQuery& q, uint32_t* types, uint32_t* classes);
 
 }  // namespace fsig

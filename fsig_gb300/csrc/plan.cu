@@ -185,6 +185,15 @@ double bfs_weight(const HostQuery& q, uint32_t root) {
 
 }  // namespace
 
+void mmatch_structure(const HostQuery& q, uint32_t* types, uint32_t* classes) {
+  const std::vector<uint32_t> t = decompose(q);
+  const Classes c = equivalent_classes(q);
+  for (uint32_t i = 0; i < q.n; i++) {
+    if (types) types[i] = t[i];
+    if (classes) classes[i] = c.inv[i].first;
+  }
+}
+
 // MMatch::generate_join_order (match/MMatch.cu:1575-1641).  Class candidate
 // counts are the counts of each class's first member.  Without a 2-core the
 // first position is restricted to the class of the forest vertex of least BFS

@@ -86,7 +86,8 @@ __global__ void __launch_bounds__(kScanThreads) scan_apply_kernel(const T* in, T
 // Exclusive scan of n elements; *total (device pointer, may be null) gets the
 // sum.  Block-sum scratch comes from the arena and is released on return.
 template <class T>
-int device_exclusive_scan(Arena& arena, const T* in, T* out, uint64_t n, T* total, cudaStream_t s) {
+int device_exclusive_scan(Arena& arena, const T* in, T* out, uint64_t n, T* total, cudaStream_t s,
+                          uint32_t* launches = nullptr) {
   if (n == 0) {
     if (total) FSIG_CUDA_TRY(cudaMemsetAsync(total, 0, sizeof(T), s));
     return FSIG_OK;
@@ -95,6 +96,7 @@ int device_exclusive_scan(Arena& arena, const T* in, T* out, uint64_t n, T* tota
   if (nb == 1) {
     scan_apply_kernel<T><<<1, kScanThreads, 0, s>>>(in, out, n, nullptr, total);
     FSIG_CUDA_TRY(cudaGetLastError());
+    if (launches) *launches += 1;
     return FSIG_OK;
   }
   uint64_t m = arena.mark();
@@ -102,10 +104,11 @@ int device_exclusive_scan(Arena& arena, const T* in, T* out, uint64_t n, T* tota
   if (!sums) return fail(FSIG_EADMISSION, "scan scratch does not fit the arena");
   scan_reduce_kernel<T><<<unsigned(nb), kScanThreads, 0, s>>>(in, n, sums);
   FSIG_CUDA_TRY(cudaGetLastError());
-  int rc = device_exclusive_scan<T>(arena, sums, sums, nb, total, s);
+  int rc = device_exclusive_scan<T>(arena, sums, sums, nb, total, s, launches);
   if (rc != FSIG_OK) return rc;
   scan_apply_kernel<T><<<unsigned(nb), kScanThreads, 0, s>>>(in, out, n, sums, nullptr);
   FSIG_CUDA_TRY(cudaGetLastError());
+  if (launches) *launches += 2;
   arena.release(m);
   return FSIG_OK;
 }

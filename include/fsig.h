@@ -45,6 +45,7 @@ extern "C" {
 #define FSIG_EIO (-7)           /* file could not be read or parsed              */
 #define FSIG_ETIMEOUT (-8)      /* a bounded device wait gave up                 */
 #define FSIG_EOVERFLOW (-9)     /* a device work queue overflowed                */
+#define FSIG_ELIMIT (-10)       /* the query exceeded its work limit              */
 
 /* algorithms (argv[3] of the reference CLI, main/run.cc:31) */
 #define FSIG_ALGO_FSIG 1  /* label+degree filter, neighbour-support refinement, core/forest/leaf order (MMatch) */
@@ -84,8 +85,15 @@ typedef struct {
   int order_source;    /* FSIG_ORDER_*                                    */
   int refine_iters;    /* neighbour-support refinement steps (-1: default) */
   int use_graph;       /* capture/replay the batch as one CUDA graph       */
-  uint32_t chunk;      /* root tasks taken per warp grab (0: autotuned)    */
-  uint32_t split_len;  /* level-1 driver range per task (0: autotuned)     */
+  uint32_t chunk;      /* tasks taken per warp grab (0: default)                  */
+  uint32_t split_len;  /* driver entries per task range (0: default)              */
+  uint64_t split_cycles; /* SM cycles on one task before its unexplored frontier
+                            is handed to idle warps (0: default)                   */
+  uint64_t max_work;     /* per-query limit on driver entries examined (all
+                            depths); a query over it stops with status
+                            FSIG_ELIMIT.  The outcome does not depend on
+                            scheduling: it is set iff the query's total work
+                            under its order exceeds the limit (0: no limit)     */
 } fsig_batch_opts;
 
 /* ---- engine lifetime; replaces GPUSubgraphMatcher::init_GPU (match/subgraph_match.h:51-80)
@@ -116,6 +124,27 @@ int fsig_match(fsig_engine* e, const fsig_query* q, int algo, fsig_result* out);
 int fsig_match_batch(fsig_engine* e, uint32_t num_queries, const fsig_query* qs,
                      const fsig_batch_opts* opts, fsig_result* out);
 
+/* ---- statistics of the engine's last fsig_match / fsig_match_batch call ----
+ * (no reference counterpart: the reference prints phase timings with its
+ * TimeRecorder, utility/time_recorder.h:26-57) */
+typedef struct {
+  uint64_t h2d_bytes;        /* host-to-device bytes copied for the call        */
+  uint64_t d2h_bytes;        /* device-to-host bytes copied back                */
+  uint64_t enum_bytes;       /* bytes the enumeration kernel's loads requested  */
+  uint32_t kernel_launches;  /* libfsig kernels launched by the call             */
+  uint32_t enum_passes;      /* enumeration kernel launches (work-splitting passes) */
+  float ms_filter;           /* device time, filter + refinement + counts       */
+  float ms_join;             /* device time, ordering + roots + enumeration     */
+  float ms_enum;             /* device time of the enumeration kernel launches  */
+  float pad;
+  uint64_t enum_tasks;       /* tasks run by the enumeration kernel             */
+  uint64_t enum_pops;        /* handed-off records taken within the same pass   */
+  uint64_t enum_handoffs;    /* frontier hand-offs                              */
+  uint64_t enum_records;     /* task records written by hand-offs               */
+  uint64_t enum_examines;    /* 32-entry driver chunks examined                 */
+} fsig_batch_stats;
+int fsig_last_stats(const fsig_engine* e, fsig_batch_stats* out);
+
 /* ---- transforms with the reference's output layout, built on the device ---- */
 /* UndirectedPlainToCSRTransformer::transform (graph_format_transformer.cc:12-37):
  * offsets[V+1], adj[2E]; rows ascending, duplicate edges kept as the reference keeps them. */
@@ -126,6 +155,16 @@ int fsig_build_csr(fsig_engine* e, uint32_t num_vertices, uint64_t num_edges,
 int fsig_build_signature(fsig_engine* e, uint32_t num_vertices, const int32_t* labels,
                          const uint32_t* offsets, const uint32_t* adj, int column_oriented,
                          uint32_t* signature);
+
+/* ---- join order on the host, no device work; replaces GSI::generate_join_order
+ *      (match/GSI.cu:105-149, algo 2 and 3) and MMatch::decompose_query_graph +
+ *      find_equivalent_classes + generate_join_order (match/MMatch.cu:543-607,
+ *      44-173, 1575-1641, algo 1), with the reference's priority-queue
+ *      tie-breaking.  candidates[n] are the per-vertex candidate counts.
+ *      vertex_types (2 core, 1 forest, 0 leaf) and classes (equivalence class
+ *      per vertex) may be NULL; they are filled for algo 1 only. ---- */
+int fsig_plan_order(const fsig_query* q, int algo, const uint32_t* candidates, uint32_t* order,
+                    uint32_t* vertex_types, uint32_t* classes);
 
 /* ---- candidate filter probe: signature_filter (match/GSI.cu:34-103) and
  *      kernel_initialise + refinement (match/MMatch.cu:609-1227) on the loaded graph.

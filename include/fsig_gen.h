@@ -23,7 +23,7 @@ extern "C" {
 
 /* Query extraction modes. */
 #define FSIG_QUERY_INDUCED 0 /* induced subgraph on a random walk's vertex set */
-#define FSIG_QUERY_DENSE 1   /* snowball walk, induced, average degree > 3      */
+#define FSIG_QUERY_DENSE 1   /* greedy walk, induced, average degree > 3 (n = 4: > 2.25) */
 #define FSIG_QUERY_SPARSE 2  /* the walk's own edges, average degree <= 3        */
 
 /* R-MAT (a, b, c, d = 1-a-b-c) over V vertices: edges[2E] receives exactly E
@@ -55,6 +55,12 @@ int fsig_gen_csr(uint32_t V, uint64_t E, const uint32_t* edges, uint32_t* offset
 int fsig_gen_query(uint32_t V, const uint32_t* offsets, const uint32_t* adj, const int32_t* labels,
                    uint32_t n, int mode, uint64_t seed, int32_t* qlabels, uint32_t* qedges,
                    uint32_t* m, uint32_t* src);
+
+/* As fsig_gen_query, with the walk confined to data vertices whose label is
+ * at least min_label (with Zipf labels: the less frequent ones). */
+int fsig_gen_query_ex(uint32_t V, const uint32_t* offsets, const uint32_t* adj, const int32_t* labels,
+                      uint32_t n, int mode, uint64_t seed, int32_t min_label, int32_t* qlabels,
+                      uint32_t* qedges, uint32_t* m, uint32_t* src);
 
 /* Write a graph in t/v/e form: "t V E", one "v id label degree" per vertex,
  * one "e u v" per edge, no trailing newline. */
