@@ -107,7 +107,8 @@ def engine_library() -> C.CDLL:
     L.fsig_plan_order.argtypes = [C.POINTER(_Query), C.c_int, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
                                   C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
     L.fsig_last_stats.argtypes = [vp, C.POINTER(_Stats)]
-    for name in ("fsig_last_stats", "fsig_plan_order", "fsig_create", "fsig_destroy", "fsig_load_graph", "fsig_load_graph_file", "fsig_graph_info",
+    L.fsig_filter_noalloc.argtypes = [vp, C.POINTER(_Query), C.c_int, C.c_void_p]
+    for name in ("fsig_filter_noalloc", "fsig_last_stats", "fsig_plan_order", "fsig_create", "fsig_destroy", "fsig_load_graph", "fsig_load_graph_file", "fsig_graph_info",
                  "fsig_match", "fsig_match_batch", "fsig_build_csr", "fsig_build_signature", "fsig_filter"):
         getattr(L, name).restype = C.c_int
     _eng = L
@@ -463,6 +464,18 @@ def select_within_budget(engine: "Engine", candidates: Sequence[Query], want: in
         if len(chosen) >= want:
             break
     return chosen[:want]
+
+
+def _filter_noalloc(self, q: Query, algo: int, d_flags: int) -> None:
+    """Candidate flags (no refinement) into the caller's device buffer at
+    address d_flags (n * V bytes), allocating nothing: for callers that cannot
+    allocate device memory at that point (see fsig_filter_noalloc)."""
+    keep = []
+    cq = _as_cquery(q, keep)
+    self._check(self._L.fsig_filter_noalloc(self._h, C.byref(cq), algo, C.c_void_p(d_flags)), "filter_noalloc")
+
+
+Engine.filter_noalloc = _filter_noalloc
 
 
 class GPUSubgraphMatcher:

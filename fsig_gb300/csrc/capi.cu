@@ -313,4 +313,16 @@ int fsig_filter(fsig_engine* h, const fsig_query* q, int algo, int refine_iters,
   return finish(h, fsig::run_filter_probe(h->e, hq, o.filter_mode, o.refine_iters, flags));
 }
 
+// Allocation-free filter: the arena is not touched; see run_filter_noalloc.
+int fsig_filter_noalloc(fsig_engine* h, const fsig_query* q, int algo, uint8_t* d_flags) {
+  int rc = select(h);
+  if (rc) return finish(h, rc);
+  if (!q || !d_flags) return finish(h, fsig::fail(FSIG_EINVAL, "null argument"));
+  if (algo != FSIG_ALGO_FSIG && algo != FSIG_ALGO_GSI && algo != FSIG_ALGO_FUSED)
+    return finish(h, fsig::fail(FSIG_EINVAL, "unknown algorithm"));
+  fsig::BatchOptions o;
+  algo_options(algo, 0, o);
+  return finish(h, fsig::run_filter_noalloc(h->e, *q, o.filter_mode, d_flags));
+}
+
 }  // extern "C"

@@ -12,6 +12,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
+#include <string>
 
 #include "match.h"
 #include "scan.cuh"
@@ -822,6 +824,154 @@ int run_filter_probe(Engine& e, const HostQuery& q, uint32_t filter_mode, int re
       }
     }
   }
+  return FSIG_OK;
+}
+
+}  // namespace fsig
+
+namespace fsig {
+
+// ---------------------------------------------------------------------------
+// Allocation-free candidate filter.
+//
+// Some callers cannot allocate device memory when they filter: a process whose
+// device memory is all handed to its own pool allocator up front has nothing
+// left for cudaMalloc, and code on a latency-critical path cannot accept the
+// device-wide synchronisation that cudaFree implies.  For them the filter can
+// run with its candidate bitmaps in the fixed array below instead of the
+// engine arena; nothing is allocated on the device or the host per call.
+//
+// The array is a file-scope device variable, so every GPU that loads this
+// library holds it until the process exits: 2^21 bitmap words (8 MiB) plus a
+// small region for the query's descriptors.  A query whose bitmaps need more
+// words is rejected with FSIG_EADMISSION.  All calls share the array and it
+// keeps the previous call's contents; each bitmap word is rewritten before it
+// is read, and the caller's flag buffer is cleared by the call.  Calls whose
+// work overlaps on the GPU (different engines or streams on one device) race
+// on the array.  The first call on a device looks up the array's address
+// (cudaGetSymbolAddress) with that device current; that first call should
+// come before any stream capture.
+// ---------------------------------------------------------------------------
+namespace {
+constexpr uint64_t kNoAllocPoolWords = 1ull << 21;
+constexpr uint64_t kNoAllocMetaWords = 8192;
+static __device__ __align__(256) uint32_t g_noalloc_scratch[kNoAllocPoolWords + kNoAllocMetaWords];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+uint32_t* g_noalloc_addr[kNoAllocMaxDevices] = {nullptr};
+
+// Device address of the scratch array on `device` (current), looked up once.
+int noalloc_scratch(int device, uint32_t** out) {
+  if (device < 0 || device >= kNoAllocMaxDevices) return fail(FSIG_EINVAL, "device index out of range");
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_addr[device]) {
+    void* p = nullptr;
+    cudaError_t err = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (err != cudaSuccess) return fail_cuda(err, "cudaGetSymbolAddress", __FILE__, __LINE__);
+    g_noalloc_addr[device] = static_cast<uint32_t*>(p);
+  }
+  *out = g_noalloc_addr[device];
+  return FSIG_OK;
+}
+
+// Bitmap words -> one flag byte per (query vertex, caller vertex id).
+__global__ void bitmap_to_flags_kernel(const QVert* __restrict__ qv, uint32_t n, const uint32_t* __restrict__ pool,
+                                       uint64_t total_words, const uint32_t* __restrict__ old_of_new, uint32_t V,
+                                       uint8_t* __restrict__ flags) {
+  for (uint64_t W = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; W < total_words;
+       W += uint64_t(gridDim.x) * blockDim.x) {
+    uint32_t u = 0;
+    while (u + 1 < n && qv[u + 1].bmoff <= W) u++;
+    uint32_t word = pool[W];
+    while (word) {
+      const uint32_t bit = __ffs(word) - 1;
+      word &= word - 1;
+      const uint32_t v = qv[u].bmbase + uint32_t((W - qv[u].bmoff) << 5) + bit;
+      if (v < V) flags[uint64_t(u) * V + old_of_new[v]] = 1;
+    }
+  }
+}
+}  // namespace
+
+int run_filter_noalloc(Engine& e, const fsig_query& q, uint32_t filter_mode, uint8_t* d_flags) {
+  if (!e.has_graph) return fail(FSIG_ENOGRAPH, "no data graph loaded");
+  const DeviceGraph& g = e.g;
+  if (q.num_vertices == 0 || q.num_vertices > uint32_t(kMaxQ)) return fail(FSIG_EQUERY, "query size must be 1..32");
+  if (!q.labels || (q.num_edges && !q.edges) || !d_flags) return fail(FSIG_EINVAL, "null argument");
+  if (g.L + 1 + kMaxQ + sizeof(QVert) / 4 * kMaxQ + 64 > kNoAllocMetaWords)
+    return fail(FSIG_EADMISSION, "the allocation-free filter supports at most 4096 labels");
+  const uint32_t n = q.num_vertices;
+  // Query descriptors on the stack (no host allocation either).
+  QVert qv[kMaxQ];
+  uint32_t adj[kMaxQ] = {0};
+  for (uint32_t e2 = 0; e2 < q.num_edges; e2++) {
+    const uint32_t a = q.edges[2 * e2], b = q.edges[2 * e2 + 1];
+    if (a >= n || b >= n) return fail(FSIG_EQUERY, "query edge endpoint out of range");
+    if (a == b) continue;
+    adj[a] |= 1u << b;
+    adj[b] |= 1u << a;
+  }
+  uint64_t words = 0;
+  for (uint32_t u = 0; u < n; u++) {
+    QVert& x = qv[u];
+    std::memset(&x, 0, sizeof(x));
+    x.label = q.labels[u];
+    x.adj = adj[u];
+    x.deg = uint32_t(__builtin_popcount(adj[u]));
+    x.u = u;
+    x.sig[0] = uint32_t(x.label);
+    for (uint32_t w = 0; w < n; w++) {
+      if (!((adj[u] >> w) & 1u)) continue;
+      uint32_t word, sh;
+      sig_slot(q.labels[w], word, sh);
+      const uint32_t cur = (x.sig[word] >> sh) & 3u;
+      x.sig[word] |= (cur == 0 ? 1u : 3u) << sh;
+    }
+    const int32_t l = x.label;
+    const uint32_t lo = (l >= 0 && l < g.L) ? g.h_base[l] : 0, hi = (l >= 0 && l < g.L) ? g.h_base[l + 1] : 0;
+    x.bmoff = words;
+    if (hi > lo) {
+      x.bmbase = lo & ~31u;
+      x.words = ((hi + 31) >> 5) - (lo >> 5);
+    }
+    words += x.words;
+  }
+  if (words > kNoAllocPoolWords)
+    return fail(FSIG_EADMISSION, "the query's candidate bitmaps need " + std::to_string(words) +
+                                     " words; the allocation-free filter holds 2^21");
+  // Label groups: query vertices sorted by label (labels present in the graph).
+  uint32_t meta[kNoAllocMetaWords];
+  uint32_t* lab_begin = meta;                 // [L + 1]
+  uint32_t* lab_gidx = meta + g.L + 1;        // [n]
+  uint32_t k = 0;
+  for (int32_t l = 0; l < g.L; l++) {
+    lab_begin[l] = k;
+    for (uint32_t u = 0; u < n; u++)
+      if (qv[u].label == l && qv[u].words) lab_gidx[k++] = u;
+  }
+  lab_begin[g.L] = k;
+  uint32_t* scratch = nullptr;
+  int rc = noalloc_scratch(e.device, &scratch);
+  if (rc) return rc;
+  uint32_t* pool = scratch;
+  // descriptors at a 16-byte aligned offset of the metadata region
+  const uint64_t meta_words = (uint64_t(g.L) + 1 + n + 3) & ~3ull;
+  uint32_t* d_meta = scratch + kNoAllocPoolWords;
+  QVert* d_qv = reinterpret_cast<QVert*>(d_meta + meta_words);
+  cudaStream_t s = e.stream;
+  FSIG_CUDA_TRY(cudaMemcpyAsync(d_meta, meta, sizeof(uint32_t) * (uint64_t(g.L) + 1 + n), cudaMemcpyHostToDevice, s));
+  FSIG_CUDA_TRY(cudaMemcpyAsync(d_qv, qv, sizeof(QVert) * n, cudaMemcpyHostToDevice, s));
+  FSIG_CUDA_TRY(cudaMemsetAsync(d_flags, 0, uint64_t(n) * g.V, s));
+  filter_kernel<<<grid_cap(uint64_t(g.V), 256, e.num_sms, 16), 256, 0, s>>>(view_of(g), d_qv, d_meta + g.L + 1,
+                                                                           d_meta, filter_mode, pool);
+  FSIG_CUDA_TRY(cudaGetLastError());
+  if (words) {
+    bitmap_to_flags_kernel<<<grid_cap(words, 256, e.num_sms, 16), 256, 0, s>>>(d_qv, n, pool, words, g.old_of_new,
+                                                                                g.V, d_flags);
+    FSIG_CUDA_TRY(cudaGetLastError());
+  }
+  FSIG_CUDA_TRY(cudaStreamSynchronize(s));
   return FSIG_OK;
 }
 

@@ -110,6 +110,10 @@ int run_batch(Engine& e, const std::vector<HostQuery>& qs, const BatchOptions& o
 // Filter (+ refinement) only; flags[n*V] in caller vertex ids, for one query.
 int run_filter_probe(Engine& e, const HostQuery& q, uint32_t filter_mode, int refine_iters, uint8_t* flags);
 
+// Filter without any allocation: bitmaps in a fixed device array, flags
+// written to the caller's device buffer (n * V bytes).
+int run_filter_noalloc(Engine& e, const fsig_query& q, uint32_t filter_mode, uint8_t* d_flags);
+
 // Host-side reference orders (plan.cpp).
 void gsi_order_host(const HostQuery& q, const uint32_t* cand, uint32_t* order);
 void mmatch_order_host(const HostQuery& q, const uint32_t* cand, uint32_t* order);

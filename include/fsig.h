@@ -171,6 +171,21 @@ int fsig_plan_order(const fsig_query* q, int algo, const uint32_t* candidates, u
  *      flags[n * V] (1 = candidate), in the caller's vertex ids. ---- */
 int fsig_filter(fsig_engine* e, const fsig_query* q, int algo, int refine_iters, uint8_t* flags);
 
+/* ---- candidate filter that allocates nothing (no counterpart in the reference).
+ *      For callers that cannot allocate device memory when they filter: a
+ *      process whose device memory is all handed to its own pool allocator,
+ *      or code on a latency-critical path that cannot accept the device-wide
+ *      synchronisation cudaFree implies.  Same result as fsig_filter with
+ *      refine_iters = 0 (no refinement), written to the caller's DEVICE buffer
+ *      d_flags[n * V] (1 = candidate, caller vertex ids); the call clears it
+ *      first.  The candidate bitmaps live in a fixed device array of 2^21
+ *      words (8 MiB) that every GPU loading the library holds until exit; a
+ *      query whose bitmaps need more returns FSIG_EADMISSION.  All calls share
+ *      the array: calls whose work overlaps on the GPU race.  The first call
+ *      on a device looks up the array's address and should come before any
+ *      stream capture.  Synchronous: the flags are complete on return. ---- */
+int fsig_filter_noalloc(fsig_engine* e, const fsig_query* q, int algo, uint8_t* d_flags);
+
 #ifdef __cplusplus
 }
 #endif
