@@ -48,7 +48,8 @@ class _Query(C.Structure):
 class _Result(C.Structure):
     _fields_ = [("count", C.c_uint64), ("hash", C.c_uint64), ("status", C.c_int32), ("num_vertices", C.c_uint32),
                 ("order", C.c_uint32 * MAX_QUERY), ("candidates", C.c_uint32 * MAX_QUERY),
-                ("level_counts", C.c_uint64 * MAX_QUERY), ("ms_filter", C.c_float), ("ms_join", C.c_float)]
+                ("level_counts", C.c_uint64 * MAX_QUERY), ("ms_filter", C.c_float), ("ms_join", C.c_float),
+                ("work", C.c_uint64)]
 
 
 class _BatchOpts(C.Structure):
@@ -75,6 +76,18 @@ def _u32p(a):
 
 def _i32p(a):
     return a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+def _f32p(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+_SINK = C.CFUNCTYPE(C.c_int, C.c_void_p, C.POINTER(C.c_uint32), C.c_uint64, C.c_uint32)
+MPNN_FEATURES = 8
+
+
+def mpnn_param_count() -> int:
+    return int(engine_library().fsig_mpnn_param_count())
 
 
 def engine_library() -> C.CDLL:
@@ -108,7 +121,25 @@ def engine_library() -> C.CDLL:
                                   C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
     L.fsig_last_stats.argtypes = [vp, C.POINTER(_Stats)]
     L.fsig_filter_noalloc.argtypes = [vp, C.POINTER(_Query), C.c_int, C.c_void_p]
-    for name in ("fsig_filter_noalloc", "fsig_last_stats", "fsig_plan_order", "fsig_create", "fsig_destroy", "fsig_load_graph", "fsig_load_graph_file", "fsig_graph_info",
+    fp = C.POINTER(C.c_float)
+    L.fsig_mpnn_param_count.restype = C.c_uint32
+    L.fsig_mpnn_param_count.argtypes = []
+    L.fsig_mpnn_set_params.argtypes = [vp, fp, C.c_uint32]
+    L.fsig_mpnn_get_params.argtypes = [vp, fp, C.c_uint32]
+    L.fsig_mpnn_features.argtypes = [vp, C.c_uint32, C.POINTER(_Query), C.c_int, C.POINTER(C.c_uint32), fp]
+    L.fsig_mpnn_forward.argtypes = [vp, C.c_uint32, C.POINTER(C.c_uint32), fp, C.POINTER(C.c_uint32), fp]
+    L.fsig_mpnn_train_step.argtypes = [vp, C.c_uint32, C.POINTER(C.c_uint32), fp, C.POINTER(C.c_uint32), fp,
+                                       C.c_float, fp, fp]
+    L.fsig_read_graph_file.argtypes = [C.c_char_p, C.c_int, C.POINTER(vp)]
+    L.fsig_graph_file_data.argtypes = [vp, C.POINTER(C.c_uint32), C.POINTER(C.POINTER(C.c_int32)),
+                                       C.POINTER(C.c_uint64), C.POINTER(C.POINTER(C.c_uint32))]
+    L.fsig_free_graph_file.argtypes = [vp]
+    L.fsig_free_graph_file.restype = None
+    L.fsig_match_embeddings.argtypes = [vp, C.POINTER(_Query), C.c_int, C.c_uint64, _SINK, vp, C.POINTER(_Result)]
+    L.fsig_write_embeddings.argtypes = [vp, C.POINTER(_Query), C.c_int, C.c_char_p, C.POINTER(_Result)]
+    for name in ("fsig_mpnn_set_params", "fsig_mpnn_get_params", "fsig_mpnn_features", "fsig_mpnn_forward",
+                 "fsig_mpnn_train_step", "fsig_read_graph_file", "fsig_graph_file_data", "fsig_match_embeddings",
+                 "fsig_write_embeddings", "fsig_filter_noalloc", "fsig_last_stats", "fsig_plan_order", "fsig_create", "fsig_destroy", "fsig_load_graph", "fsig_load_graph_file", "fsig_graph_info",
                  "fsig_match", "fsig_match_batch", "fsig_build_csr", "fsig_build_signature", "fsig_filter"):
         getattr(L, name).restype = C.c_int
     _eng = L
@@ -205,6 +236,7 @@ class Result:
     level_counts: list
     ms_filter: float = 0.0
     ms_join: float = 0.0
+    work: int = 0
 
 
 def read_graph(path, is_labeled: bool = True) -> Graph:
@@ -324,7 +356,7 @@ def _as_cquery(q: Query, keep: list) -> _Query:
 def _result(r: _Result) -> Result:
     n = r.num_vertices
     return Result(int(r.count), int(r.hash), int(r.status), list(r.order[:n]), list(r.candidates[:n]),
-                  [int(x) for x in r.level_counts[:n]], float(r.ms_filter), float(r.ms_join))
+                  [int(x) for x in r.level_counts[:n]], float(r.ms_filter), float(r.ms_join), int(r.work))
 
 
 class Engine:
@@ -433,6 +465,80 @@ class Engine:
         self._check(self._L.fsig_filter(self._h, C.byref(cq), algo, refine_iters,
                                         out.ctypes.data_as(C.POINTER(C.c_uint8))), "filter")
         return out.reshape(q.num_vertices, V)
+
+    # embeddings (EmbeddingWriter)
+    def match_embeddings(self, q: Query, algo: int = ALGO_FSIG, buffer_rows: int = 0):
+        """(Result, rows[count, n]): every embedding, column u = the data
+        vertex of query vertex u, in no particular row order."""
+        keep = []
+        cq = _as_cquery(q, keep)
+        chunks = []
+
+        def sink(_user, rows, num, width):
+            chunks.append(np.ctypeslib.as_array(rows, shape=(int(num) * int(width),)).copy().reshape(-1, width))
+            return 0
+
+        cb = _SINK(sink)
+        r = _Result()
+        self._check(self._L.fsig_match_embeddings(self._h, C.byref(cq), algo, buffer_rows, cb, None, C.byref(r)),
+                    "match_embeddings")
+        n = q.num_vertices
+        rows = np.concatenate(chunks) if chunks else np.zeros((0, n), np.uint32)
+        return _result(r), rows
+
+    def write_embeddings(self, q: Query, path, algo: int = ALGO_FSIG) -> Result:
+        keep = []
+        cq = _as_cquery(q, keep)
+        r = _Result()
+        self._check(self._L.fsig_write_embeddings(self._h, C.byref(cq), algo, str(path).encode(), C.byref(r)),
+                    "write_embeddings")
+        return _result(r)
+
+    # order-scoring network (ORDER_LEARNED)
+    def mpnn_set_params(self, params: np.ndarray) -> None:
+        p = np.ascontiguousarray(params, np.float32)
+        self._check(self._L.fsig_mpnn_set_params(self._h, _f32p(p), p.size), "mpnn_set_params")
+
+    def mpnn_get_params(self) -> np.ndarray:
+        p = np.zeros(mpnn_param_count(), np.float32)
+        self._check(self._L.fsig_mpnn_get_params(self._h, _f32p(p), p.size), "mpnn_get_params")
+        return p
+
+    def mpnn_features(self, qs: Sequence[Query], candidates: Sequence, algo: int = ALGO_FUSED) -> np.ndarray:
+        """Device-computed features [total vertices, 8] from candidate counts
+        and algo's heuristic order."""
+        keep = []
+        arr = (_Query * max(len(qs), 1))()
+        for i, q in enumerate(qs):
+            arr[i] = _as_cquery(q, keep)
+        cand = np.ascontiguousarray(np.concatenate([np.asarray(c, np.uint32) for c in candidates])
+                                    if len(candidates) else np.zeros(1, np.uint32), np.uint32)
+        G = sum(q.num_vertices for q in qs)
+        out = np.zeros(max(G, 1) * MPNN_FEATURES, np.float32)
+        self._check(self._L.fsig_mpnn_features(self._h, len(qs), arr, algo, _u32p(cand), _f32p(out)),
+                    "mpnn_features")
+        return out[: G * MPNN_FEATURES].reshape(G, MPNN_FEATURES)
+
+    def mpnn_forward(self, node_offsets, features, neighbours) -> np.ndarray:
+        off = np.ascontiguousarray(node_offsets, np.uint32)
+        f = np.ascontiguousarray(features, np.float32).reshape(-1)
+        nb = np.ascontiguousarray(neighbours, np.uint32)
+        out = np.zeros(max(int(off[-1]), 1), np.float32)
+        self._check(self._L.fsig_mpnn_forward(self._h, len(off) - 1, _u32p(off), _f32p(f), _u32p(nb), _f32p(out)),
+                    "mpnn_forward")
+        return out[: int(off[-1])]
+
+    def mpnn_train_step(self, node_offsets, features, neighbours, targets, lr: float = 0.0):
+        """One step on the mean squared error: (loss, gradients), Adam update if lr > 0."""
+        off = np.ascontiguousarray(node_offsets, np.uint32)
+        f = np.ascontiguousarray(features, np.float32).reshape(-1)
+        nb = np.ascontiguousarray(neighbours, np.uint32)
+        t = np.ascontiguousarray(targets, np.float32)
+        loss = np.zeros(1, np.float32)
+        grads = np.zeros(mpnn_param_count(), np.float32)
+        self._check(self._L.fsig_mpnn_train_step(self._h, len(off) - 1, _u32p(off), _f32p(f), _u32p(nb), _f32p(t),
+                                                 float(lr), _f32p(loss), _f32p(grads)), "mpnn_train_step")
+        return float(loss[0]), grads
 
 
 def plan_order(q: Query, algo: int, candidates) -> dict:

@@ -1,4 +1,5 @@
 // C ABI of libfsig (include/fsig.h).
+#include <cstdio>
 #include <cstring>
 #include <new>
 #include <string>
@@ -6,6 +7,7 @@
 
 #include "engine.h"
 #include "match.h"
+#include "mpnn.h"
 #include "reader.h"
 
 namespace fsig {
@@ -28,6 +30,10 @@ void clear_thread_error() { t_err.clear(); }
 }  // namespace fsig
 
 using fsig::Engine;
+
+struct fsig_graph_file {
+  fsig::TveGraph g;
+};
 
 struct fsig_engine {
   Engine e;
@@ -61,6 +67,7 @@ void fill_result(const fsig::HostQuery& hq, const fsig::BatchOutput& o, uint32_t
   }
   r->ms_filter = o.ms_filter;
   r->ms_join = o.ms_join;
+  r->work = o.res[qi].work;
 }
 
 void algo_options(int algo, int refine_iters, fsig::BatchOptions& o) {
@@ -162,6 +169,7 @@ int fsig_destroy(fsig_engine* h) {
     if (ev) cudaEventDestroy(ev);
   for (auto& ev : h->e.ev_enum)
     if (ev) cudaEventDestroy(ev);
+  fsig::mpnn_free(h->e);
   if (h->e.arena.base) cudaFree(h->e.arena.base);
   if (h->e.pinned) cudaFreeHost(h->e.pinned);
   if (h->e.stream) cudaStreamDestroy(h->e.stream);
@@ -222,6 +230,98 @@ int fsig_match(fsig_engine* h, const fsig_query* q, int algo, fsig_result* out) 
   return FSIG_OK;
 }
 
+int fsig_read_graph_file(const char* path, int is_labeled, fsig_graph_file** out) {
+  fsig::clear_thread_error();
+  if (!path || !out) return FSIG_EINVAL;
+  *out = nullptr;
+  auto* f = new (std::nothrow) fsig_graph_file();
+  if (!f) return FSIG_EINVAL;
+  std::string err;
+  if (fsig::read_tve(path, is_labeled, f->g, err) != 0) {
+    delete f;
+    fsig::fail(FSIG_EIO, err);
+    return FSIG_EIO;
+  }
+  *out = f;
+  return FSIG_OK;
+}
+
+int fsig_graph_file_data(const fsig_graph_file* f, uint32_t* V, const int32_t** labels, uint64_t* E,
+                         const uint32_t** edges) {
+  if (!f) return FSIG_EINVAL;
+  if (V) *V = f->g.num_vertices;
+  if (labels) *labels = f->g.labels.data();
+  if (E) *E = f->g.edges.size() / 2;
+  if (edges) *edges = f->g.edges.data();
+  return FSIG_OK;
+}
+
+void fsig_free_graph_file(fsig_graph_file* f) { delete f; }
+
+int fsig_match_embeddings(fsig_engine* h, const fsig_query* q, int algo, uint64_t buffer_rows,
+                          fsig_embedding_sink sink, void* user, fsig_result* out) {
+  int rc = select(h);
+  if (rc) return finish(h, rc);
+  if (!q || !out || !sink) return finish(h, fsig::fail(FSIG_EINVAL, "null argument"));
+  if (algo != FSIG_ALGO_FSIG && algo != FSIG_ALGO_GSI && algo != FSIG_ALGO_FUSED)
+    return finish(h, fsig::fail(FSIG_EINVAL, "unknown algorithm"));
+  std::memset(out, 0, sizeof(*out));
+  fsig::HostQuery hq;
+  rc = fsig::prepare_query(*q, h->e.has_graph ? h->e.g.L : 0, hq);
+  if (rc) { out->status = rc; return finish(h, rc); }
+  fsig::BatchOptions o;
+  algo_options(algo, -1, o);
+  if (!hq.has_given) o.host_order = algo == FSIG_ALGO_FSIG ? fsig::mmatch_order_host : fsig::gsi_order_host;
+  else o.order_mode = fsig::kOrderGiven;
+  fsig::BatchOutput bo;
+  rc = fsig::run_embeddings(h->e, hq, o, buffer_rows ? buffer_rows : (1ull << 20), sink, user, bo);
+  if (rc) { out->status = rc; return finish(h, rc); }
+  fill_result(hq, bo, 0, 0, out);
+  return FSIG_OK;
+}
+
+namespace {
+struct TextSink {
+  FILE* fp;
+  std::vector<char> buf;
+  bool failed = false;
+};
+
+int text_sink(void* user, const uint32_t* rows, uint64_t num_rows, uint32_t width) {
+  auto* t = static_cast<TextSink*>(user);
+  t->buf.clear();
+  t->buf.reserve(num_rows * width * 11);
+  char tmp[12];
+  for (uint64_t r = 0; r < num_rows; r++) {
+    for (uint32_t c = 0; c < width; c++) {
+      uint32_t v = rows[r * width + c];
+      int k = 0;
+      do { tmp[k++] = char('0' + v % 10); v /= 10; } while (v);
+      while (k) t->buf.push_back(tmp[--k]);
+      t->buf.push_back(c + 1 == width ? '\n' : ' ');
+    }
+  }
+  if (std::fwrite(t->buf.data(), 1, t->buf.size(), t->fp) != t->buf.size()) {
+    t->failed = true;
+    return 1;
+  }
+  return 0;
+}
+}  // namespace
+
+int fsig_write_embeddings(fsig_engine* h, const fsig_query* q, int algo, const char* path, fsig_result* out) {
+  if (!h) return FSIG_EINVAL;
+  if (!path) return finish(h, fsig::fail(FSIG_EINVAL, "no path"));
+  TextSink t;
+  t.fp = std::fopen(path, "wb");
+  if (!t.fp) return finish(h, fsig::fail(FSIG_EIO, std::string("cannot open ") + path));
+  int rc = fsig_match_embeddings(h, q, algo, 0, text_sink, &t, out);
+  if (std::fclose(t.fp) != 0) t.failed = true;
+  if (rc) return rc;
+  if (t.failed) return finish(h, fsig::fail(FSIG_EIO, std::string("cannot write ") + path));
+  return FSIG_OK;
+}
+
 int fsig_match_batch(fsig_engine* h, uint32_t nq, const fsig_query* qs, const fsig_batch_opts* opts,
                      fsig_result* out) {
   int rc = select(h);
@@ -246,7 +346,10 @@ int fsig_match_batch(fsig_engine* h, uint32_t nq, const fsig_query* qs, const fs
   fsig::BatchOptions o;
   algo_options(bo.algo, bo.refine_iters, o);
   if (bo.order_source == FSIG_ORDER_GIVEN) o.order_mode = fsig::kOrderGiven;
-  else if (bo.order_source == FSIG_ORDER_LEARNED) return finish(h, fsig::fail(FSIG_EINVAL, "no order network loaded"));
+  else if (bo.order_source == FSIG_ORDER_LEARNED) {
+    if (!h->e.mpnn || !h->e.mpnn->loaded) return finish(h, fsig::fail(FSIG_EINVAL, "no order network loaded"));
+    o.learned = true;
+  }
   if (bo.chunk) o.chunk = bo.chunk;
   if (bo.split_len) o.split = bo.split_len;
   if (bo.split_cycles) o.budget_cycles = (long long)bo.split_cycles;
@@ -260,6 +363,53 @@ int fsig_match_batch(fsig_engine* h, uint32_t nq, const fsig_query* qs, const fs
     g0 += hq[k].n;
   }
   return FSIG_OK;
+}
+
+uint32_t fsig_mpnn_param_count(void) { return uint32_t(fsig::kParams); }
+
+int fsig_mpnn_set_params(fsig_engine* h, const float* params, uint32_t count) {
+  int rc = select(h);
+  if (rc) return finish(h, rc);
+  if (!params || count != uint32_t(fsig::kParams)) return finish(h, fsig::fail(FSIG_EINVAL, "parameter count"));
+  return finish(h, fsig::mpnn_set_params(h->e, params));
+}
+
+int fsig_mpnn_get_params(fsig_engine* h, float* params, uint32_t count) {
+  int rc = select(h);
+  if (rc) return finish(h, rc);
+  if (!params || count != uint32_t(fsig::kParams)) return finish(h, fsig::fail(FSIG_EINVAL, "parameter count"));
+  return finish(h, fsig::mpnn_get_params(h->e, params));
+}
+
+int fsig_mpnn_features(fsig_engine* h, uint32_t nq, const fsig_query* qs, int algo, const uint32_t* cand,
+                       float* features) {
+  int rc = select(h);
+  if (rc) return finish(h, rc);
+  if (nq && (!qs || !cand || !features)) return finish(h, fsig::fail(FSIG_EINVAL, "null argument"));
+  std::vector<fsig::HostQuery> hq(nq);
+  for (uint32_t i = 0; i < nq; i++) {
+    rc = fsig::prepare_query(qs[i], h->e.has_graph ? h->e.g.L : 0, hq[i]);
+    if (rc) return finish(h, rc);
+  }
+  fsig::BatchOptions o;
+  algo_options(algo, -1, o);
+  return finish(h, fsig::run_features(h->e, hq, cand, o.order_mode, features));
+}
+
+int fsig_mpnn_forward(fsig_engine* h, uint32_t ng, const uint32_t* goff, const float* feat, const uint32_t* nbr,
+                      float* scores) {
+  int rc = select(h);
+  if (rc) return finish(h, rc);
+  if (!goff || (goff[ng] && (!feat || !nbr || !scores))) return finish(h, fsig::fail(FSIG_EINVAL, "null argument"));
+  return finish(h, fsig::mpnn_run(h->e, ng, goff, feat, nbr, nullptr, 0.f, scores, nullptr, nullptr));
+}
+
+int fsig_mpnn_train_step(fsig_engine* h, uint32_t ng, const uint32_t* goff, const float* feat, const uint32_t* nbr,
+                         const float* targets, float lr, float* loss, float* grads) {
+  int rc = select(h);
+  if (rc) return finish(h, rc);
+  if (!goff || !targets || (goff[ng] && (!feat || !nbr))) return finish(h, fsig::fail(FSIG_EINVAL, "null argument"));
+  return finish(h, fsig::mpnn_run(h->e, ng, goff, feat, nbr, targets, lr, nullptr, loss, grads));
 }
 
 int fsig_last_stats(const fsig_engine* h, fsig_batch_stats* out) {

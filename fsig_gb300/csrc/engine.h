@@ -53,6 +53,7 @@ struct Engine {
   fsig_batch_stats last{};
   uint64_t cur_h2d = 0;  // host-to-device bytes of the call in progress
   unsigned long long last_ev[8] = {0};  // enumeration event counters of the last call
+  struct MpnnState* mpnn = nullptr;      // order-scoring network (mpnn.cu), created on first use
 };
 
 // graph_store.cu

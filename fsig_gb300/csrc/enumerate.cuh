@@ -51,6 +51,7 @@ struct EnumArgs {
   const uint32_t* __restrict__ chunk_off;  // [nroots + 1]
   uint32_t nroots;
   uint32_t split;
+  uint32_t t_end;  // pass-0 tasks [initial ctr[0], t_end) (a range of the task space)
   // explicit input tasks (passes >= 1)
   const TaskRec* __restrict__ in_tasks;
   uint32_t in_count;
@@ -68,6 +69,12 @@ struct EnumArgs {
   unsigned long long* algo_bytes;
   unsigned long long* ev;       // event counters: tasks, records popped, hand-offs, records written, examines
   unsigned long long seed;
+  // optional embedding output (single-query batches): rows of n caller ids,
+  // column u = the data vertex of query vertex u; emit_ctr counts every
+  // embedding found, rows past emit_cap are not written
+  uint32_t* emit;
+  unsigned long long emit_cap;
+  unsigned long long* emit_ctr;
 };
 
 constexpr uint32_t kErrTimeout = 1u;
@@ -124,7 +131,7 @@ __global__ void __launch_bounds__(256) enumerate_kernel(EnumArgs A) {
   const uint32_t lane = threadIdx.x & 31;
   const GraphView& g = A.g;
   const uint64_t W1 = uint64_t(g.L) + 1;
-  const uint32_t T_in = A.in_tasks ? A.in_count : A.chunk_off[A.nroots];
+  const uint32_t T_in = A.in_tasks ? A.in_count : min(A.chunk_off[A.nroots], A.t_end);
 
   // lane-distributed level state
   uint32_t f = 0, dpos = 0, dend = 0, drv = 0, cnt = 0, it = 0;
@@ -348,6 +355,29 @@ __global__ void __launch_bounds__(256) enumerate_kernel(EnumArgs A) {
     return __shfl_sync(kFull, w, 0) != 0;
   };
 
+  // Writes the embeddings completed by one leaf examine step: lanes in m hold
+  // a leaf's caller id in xo, lanes < lv the shared prefix (f).
+  auto emit_rows = [&](uint32_t m, uint32_t lv, uint32_t xo) {
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(A.emit_ctr, (unsigned long long)__popc(m));
+    base = __shfl_sync(kFull, base, 0);
+    const uint32_t n = lv + 1;
+    const uint32_t col = lane < n ? uint32_t(ws.plan.qv[lane]) : 0u;
+    const uint32_t fo = lane < lv ? __ldg(g.old_of_new + f) : 0u;
+    uint32_t k = 0;
+    while (m) {
+      const uint32_t b = __ffs(m) - 1;
+      m &= m - 1;
+      const uint32_t leaf = __shfl_sync(kFull, xo, b);
+      const unsigned long long row = base + k++;
+      if (row < A.emit_cap) {
+        uint32_t* dst = A.emit + row * n;
+        if (lane < lv) dst[col] = fo;
+        else if (lane == lv) dst[col] = leaf;
+      }
+    }
+  };
+
   // Runs one task: depth d, mapped f (lane-distributed, lanes < d), driver
   // range override [lo, hi) at depth d.
   auto run = [&](uint32_t d, uint32_t lo_set, uint32_t hi_set) {
@@ -371,6 +401,10 @@ __global__ void __launch_bounds__(256) enumerate_kernel(EnumArgs A) {
       if (lane == 0) {
         my_count += 1;
         my_hash += fmix64(A.seed + Sn);
+        if (A.emit) {
+          const unsigned long long row = atomicAdd(A.emit_ctr, 1ull);
+          if (row < A.emit_cap) A.emit[row] = __ldg(g.old_of_new + f);
+        }
       }
       return;
     }
@@ -395,6 +429,7 @@ __global__ void __launch_bounds__(256) enumerate_kernel(EnumArgs A) {
             my_count += 1;
             my_hash += fmix64(A.seed + Sp + fmix64(tb | xo));
           }
+          if (A.emit && m) emit_rows(m, lv, xo);
           if (lane == lv) lc += __popc(m);
           if ((++steps & 63u) == 0) {
             if (over_limit()) return;

@@ -16,6 +16,7 @@
 #include <string>
 
 #include "match.h"
+#include "mpnn.h"
 #include "scan.cuh"
 
 namespace fsig {
@@ -544,7 +545,8 @@ constexpr uint32_t kOverflowCap = 1u << 20;  // task records per overflow queue
 int enumerate_passes(Engine& e, const BatchOptions& opt, const GraphView& gv, const Plan* d_plans,
                      const uint32_t* pool, uint32_t Q, const uint32_t* d_roots, const uint32_t* d_root_q,
                      const uint32_t* d_chunk_off, uint32_t nroots, uint32_t split, QueryResult* d_res,
-                     unsigned long long* d_misc, uint32_t& passes, float& ms_enum, uint64_t& d2h) {
+                     unsigned long long* d_misc, uint32_t* d_emit, unsigned long long* d_emit_ctr,
+                     uint32_t& passes, float& ms_enum, uint64_t& d2h) {
   cudaStream_t s = e.stream;
   TaskRec* qa = e.arena.take<TaskRec>(kOverflowCap);
   TaskRec* qb = e.arena.take<TaskRec>(kOverflowCap);
@@ -575,6 +577,10 @@ int enumerate_passes(Engine& e, const BatchOptions& opt, const GraphView& gv, co
   A.chunk_off = d_chunk_off;
   A.nroots = nroots;
   A.split = split;
+  A.t_end = opt.task_end;
+  A.emit = d_emit;
+  A.emit_cap = d_emit ? opt.emit_cap : 0;
+  A.emit_ctr = d_emit_ctr;
   A.in_tasks = nullptr;
   A.in_count = 0;
   A.out_cap = kOverflowCap;
@@ -601,6 +607,7 @@ int enumerate_passes(Engine& e, const BatchOptions& opt, const GraphView& gv, co
     A.budget = (long long)opt.budget_cycles;
     // every warp starts active; idle warps are counted as they wait
     uint32_t init[8 * kCtrStride] = {0};
+    init[0] = pass == 0 ? opt.task_begin : 0u;
     init[5 * kCtrStride] = uint32_t(e.num_sms * per_sm) * wpb;
     FSIG_CUDA_TRY(cudaMemcpyAsync(ctr, init, sizeof(init), cudaMemcpyHostToDevice, s));
     FSIG_CUDA_TRY(cudaEventRecord(e.ev_enum[0], s));
@@ -712,6 +719,25 @@ int run_batch(Engine& e, const std::vector<HostQuery>& qs, const BatchOptions& o
     e.cur_h2d += sizeof(uint32_t) * b.G;
     order_mode = kOrderGiven;
   }
+  const float* d_score_src = d_scores;
+  if (opt.learned) {
+    // Order-network scores from the filtered candidate counts, on the device;
+    // the algorithm's own heuristic order is one of the inputs.
+    float* d_feat = e.arena.take<float>(uint64_t(std::max<uint32_t>(b.G, 1)) * kFeat);
+    uint32_t* d_nbr = e.arena.take<uint32_t>(std::max<uint32_t>(b.G, 1));
+    float* d_lscores = e.arena.take<float>(std::max<uint32_t>(b.G, 1));
+    if (!d_feat || !d_nbr || !d_lscores) return fail(FSIG_EADMISSION, "order-network inputs do not fit the arena");
+    order_kernel<<<(Q + 7) / 8, 256, 0, s>>>(d_qv, d_qoff, Q, d_counts, order_mode, d_scores, d_given, d_plans,
+                                             d_rootcnt, d_orders);
+    FSIG_CUDA_TRY(cudaGetLastError());
+    rc = mpnn_features_device(e, d_qv, b.G, d_qoff, Q, d_counts, d_orders, d_feat, d_nbr);
+    if (rc) return rc;
+    rc = mpnn_forward_device(e, Q, d_qoff, d_feat, d_nbr, d_lscores);
+    if (rc) return rc;
+    launches += 3;
+    d_score_src = d_lscores;
+    order_mode = kOrderScores;
+  }
   uint32_t* d_roots = e.arena.take<uint32_t>(std::max<uint64_t>(b.root_cap, 1));
   uint32_t* d_root_q = e.arena.take<uint32_t>(std::max<uint64_t>(b.root_cap, 1));
   uint32_t* d_chunks = e.arena.take<uint32_t>(std::max<uint64_t>(b.root_cap, 1) + 1);
@@ -719,7 +745,7 @@ int run_batch(Engine& e, const std::vector<HostQuery>& qs, const BatchOptions& o
   if (!d_roots || !d_root_q || !d_chunks || !d_chunk_off)
     return fail(FSIG_EADMISSION, "root list does not fit the device arena");
   FSIG_CUDA_TRY(cudaMemsetAsync(d_rootcnt, 0, sizeof(uint32_t) * (uint64_t(Q) + 1), s));
-  order_kernel<<<(Q + 7) / 8, 256, 0, s>>>(d_qv, d_qoff, Q, d_counts, order_mode, d_scores, d_given, d_plans,
+  order_kernel<<<(Q + 7) / 8, 256, 0, s>>>(d_qv, d_qoff, Q, d_counts, order_mode, d_score_src, d_given, d_plans,
                                            d_rootcnt, d_orders);
   FSIG_CUDA_TRY(cudaGetLastError());
   rc = device_exclusive_scan<uint32_t>(e.arena, d_rootcnt, d_rootoff, uint64_t(Q) + 1, nullptr, s, &launches);
@@ -744,9 +770,29 @@ int run_batch(Engine& e, const std::vector<HostQuery>& qs, const BatchOptions& o
   rc = device_exclusive_scan<uint32_t>(e.arena, d_chunks, d_chunk_off, uint64_t(nroots) + 1, nullptr, s, &launches);
   if (rc) return rc;
   FSIG_CUDA_TRY(cudaMemsetAsync(d_res, 0, sizeof(QueryResult) * Q, s));
+  uint32_t* d_emit = nullptr;
+  unsigned long long* d_emit_ctr = nullptr;
+  if (opt.emit_cap) {
+    if (Q != 1) return fail(FSIG_EINVAL, "embedding output is for one query at a time");
+    d_emit_ctr = e.arena.take<unsigned long long>(1);
+    d_emit = e.arena.take<uint32_t>(opt.emit_cap * qs[0].n);
+    if (!d_emit || !d_emit_ctr) return fail(FSIG_EADMISSION, "embedding buffer does not fit the device arena");
+    FSIG_CUDA_TRY(cudaMemsetAsync(d_emit_ctr, 0, sizeof(unsigned long long), s));
+  }
   rc = enumerate_passes(e, opt, view_of(g), d_plans, pool, Q, d_roots, d_root_q, d_chunk_off, nroots, split, d_res,
-                        d_misc, out.passes, out.ms_enum, d2h);
+                        d_misc, d_emit, d_emit_ctr, out.passes, out.ms_enum, d2h);
   if (rc) return rc;
+  if (opt.emit_cap) {
+    FSIG_CUDA_TRY(cudaMemcpyAsync(&out.emit_total, d_emit_ctr, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+    FSIG_CUDA_TRY(cudaMemcpyAsync(&out.tasks_total, d_chunk_off + nroots, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    FSIG_CUDA_TRY(cudaStreamSynchronize(s));
+    const uint64_t rows = std::min<uint64_t>(out.emit_total, opt.emit_cap);
+    out.rows.resize(rows * qs[0].n);
+    if (rows)
+      FSIG_CUDA_TRY(cudaMemcpyAsync(out.rows.data(), d_emit, sizeof(uint32_t) * rows * qs[0].n,
+                                    cudaMemcpyDeviceToHost, s));
+    d2h += 12 + sizeof(uint32_t) * rows * qs[0].n;
+  }
   launches += out.passes;
   FSIG_CUDA_TRY(cudaEventRecord(e.ev[2], s));
 
@@ -779,6 +825,86 @@ int run_batch(Engine& e, const std::vector<HostQuery>& qs, const BatchOptions& o
   e.last.enum_records = e.last_ev[3];
   e.last.enum_examines = e.last_ev[4];
   e.arena.release(g.arena_mark);
+  return FSIG_OK;
+}
+
+int run_embeddings(Engine& e, const HostQuery& q, BatchOptions opt, uint64_t buffer_rows,
+                   int (*sink)(void*, const uint32_t*, uint64_t, uint32_t), void* user, BatchOutput& first) {
+  if (!buffer_rows) return fail(FSIG_EINVAL, "embedding buffer of zero rows");
+  const std::vector<HostQuery> qs(1, q);
+  opt.emit_cap = buffer_rows;
+  opt.task_begin = 0;
+  opt.task_end = 0xffffffffu;
+  int rc = run_batch(e, qs, opt, first);
+  if (rc) return rc;
+  if (!first.ok[0] || first.res[0].aborted) return FSIG_OK;
+  if (first.emit_total <= buffer_rows) {
+    if (first.emit_total) sink(user, first.rows.data(), first.emit_total, q.n);
+    return FSIG_OK;
+  }
+  // More embeddings than one buffer holds: cut the task space into ranges,
+  // matched one after the other, halving a range whose rows still overflow.
+  first.rows.clear();
+  const uint64_t total = first.res[0].count;
+  const uint32_t T = first.tasks_total;
+  const uint64_t parts = std::max<uint64_t>(1, std::min<uint64_t>(T, 2 * ((total + buffer_rows - 1) / buffer_rows)));
+  std::vector<std::pair<uint32_t, uint32_t>> todo;
+  for (uint64_t i = parts; i-- > 0;) todo.push_back({uint32_t(T * i / parts), uint32_t(T * (i + 1) / parts)});
+  uint64_t seen = 0;
+  while (!todo.empty()) {
+    const auto [t0, t1] = todo.back();
+    todo.pop_back();
+    if (t0 >= t1) continue;
+    BatchOutput o;
+    opt.task_begin = t0;
+    opt.task_end = t1;
+    rc = run_batch(e, qs, opt, o);
+    if (rc) return rc;
+    if (o.emit_total > buffer_rows) {
+      if (t1 - t0 == 1) return fail(FSIG_EADMISSION, "the embeddings under one root chunk exceed the row buffer");
+      const uint32_t mid = t0 + (t1 - t0) / 2;
+      todo.push_back({mid, t1});
+      todo.push_back({t0, mid});
+      continue;
+    }
+    seen += o.emit_total;
+    if (o.emit_total && sink(user, o.rows.data(), o.emit_total, q.n)) return FSIG_OK;
+  }
+  if (seen != total) return fail(FSIG_ECUDA, "task ranges found a different number of embeddings");
+  return FSIG_OK;
+}
+
+int run_features(Engine& e, const std::vector<HostQuery>& qs, const uint32_t* counts, uint32_t order_mode,
+                 float* features) {
+  if (!e.has_graph) return fail(FSIG_ENOGRAPH, "no data graph loaded");
+  BatchLayout b;
+  layout_batch(e.g, qs, b);
+  const uint64_t mark = e.arena.mark();
+  int rc = FSIG_OK;
+  QVert* d_qv = upload(e, b.qv, rc);
+  if (rc) return rc;
+  uint32_t* d_qoff = upload(e, b.qoff, rc);
+  if (rc) return rc;
+  std::vector<uint32_t> hc(counts, counts + b.G);
+  uint32_t* d_counts = upload(e, hc, rc);
+  if (rc) return rc;
+  float* d_feat = e.arena.take<float>(uint64_t(std::max<uint32_t>(b.G, 1)) * kFeat);
+  uint32_t* d_nbr = e.arena.take<uint32_t>(std::max<uint32_t>(b.G, 1));
+  Plan* d_plans = e.arena.take<Plan>(std::max<uint32_t>(b.Q, 1));
+  uint32_t* d_rootcnt = e.arena.take<uint32_t>(uint64_t(b.Q) + 1);
+  uint32_t* d_orders = e.arena.take<uint32_t>(uint64_t(std::max<uint32_t>(b.Q, 1)) * kMaxQ);
+  if (!d_feat || !d_nbr || !d_plans || !d_rootcnt || !d_orders) return fail(FSIG_EADMISSION, "arena");
+  if (b.Q) {
+    order_kernel<<<(b.Q + 7) / 8, 256, 0, e.stream>>>(d_qv, d_qoff, b.Q, d_counts, order_mode, nullptr, nullptr,
+                                                      d_plans, d_rootcnt, d_orders);
+    FSIG_CUDA_TRY(cudaGetLastError());
+  }
+  rc = mpnn_features_device(e, d_qv, b.G, d_qoff, b.Q, d_counts, d_orders, d_feat, d_nbr);
+  if (rc) return rc;
+  if (b.G)
+    FSIG_CUDA_TRY(cudaMemcpyAsync(features, d_feat, sizeof(float) * kFeat * b.G, cudaMemcpyDeviceToHost, e.stream));
+  FSIG_CUDA_TRY(cudaStreamSynchronize(e.stream));
+  e.arena.release(mark);
   return FSIG_OK;
 }
 

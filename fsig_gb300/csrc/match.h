@@ -86,6 +86,11 @@ struct BatchOptions {
   unsigned long long max_work = 0;  // per-query limit on examined driver entries (0: none)
   uint32_t warps_per_block = 8;
   const float* scores = nullptr;  // host scores per query vertex (kOrderScores), batch order
+  bool learned = false;           // score with the loaded order network (kOrderScores)
+  // Single-query batches only: write up to emit_cap embeddings to
+  // BatchOutput::rows, and enumerate only pass-0 tasks [task_begin, task_end).
+  uint64_t emit_cap = 0;
+  uint32_t task_begin = 0, task_end = 0xffffffffu;
   // When set, candidate counts are brought to the host after filtering and
   // this function chooses each query's order (the reference-exact orders).
   void (*host_order)(const HostQuery&, const uint32_t* cand, uint32_t* order) = nullptr;
@@ -102,10 +107,25 @@ struct BatchOutput {
   uint64_t h2d_bytes = 0, d2h_bytes = 0;
   uint32_t launches = 0;
   float ms_enum = 0;
+  std::vector<uint32_t> rows;   // emitted embeddings, n per row (emit_cap > 0)
+  uint64_t emit_total = 0;      // embeddings found in the task range
+  uint32_t tasks_total = 0;     // size of the pass-0 task space (emit_cap > 0)
 };
 
 // Runs filter -> refine -> order -> roots -> enumerate for a batch.
 int run_batch(Engine& e, const std::vector<HostQuery>& qs, const BatchOptions& opt, BatchOutput& out);
+
+// All embeddings of one query, handed to sink in chunks of at most
+// buffer_rows rows (n caller ids per row, column u = query vertex u).  When
+// they do not fit one buffer the pass-0 task space is cut into ranges that
+// each fit, each range matched separately.  A non-zero sink return stops.
+int run_embeddings(Engine& e, const HostQuery& q, BatchOptions opt, uint64_t buffer_rows,
+                   int (*sink)(void*, const uint32_t*, uint64_t, uint32_t), void* user, BatchOutput& first);
+
+// Features of the given queries from host candidate counts and the device
+// heuristic order of order_mode (device kernels).
+int run_features(Engine& e, const std::vector<HostQuery>& qs, const uint32_t* counts, uint32_t order_mode,
+                 float* features);
 
 // Filter (+ refinement) only; flags[n*V] in caller vertex ids, for one query.
 int run_filter_probe(Engine& e, const HostQuery& q, uint32_t filter_mode, int refine_iters, uint8_t* flags);

@@ -1,0 +1,262 @@
+"""Learned matching order: parameters of the order-scoring network, the
+order/cost logs the engine produces, and training with the engine's own
+forward and backward kernels (``fsig_mpnn_train_step``).
+
+The reference has no counterpart: it orders by heuristics only
+(match/GSI.cu:105-149, match/MMatch.cu:1575-1641).  Here the heuristic order
+stays the fallback and the judge of cost:
+
+* a log records, per query, the heuristic order and a set of alternative
+  connected orders, each with the driver entries its enumeration examined
+  (``work``, deterministic) and its per-level intermediate counts;
+  alternatives run under a work limit equal to the heuristic's own work, so an
+  alternative that is not better stops early and a log costs at most
+  (alternatives + 1) heuristic runs;
+* the network sees the heuristic order (each vertex's position in it) among
+  its inputs, so it learns corrections to that order;
+* the training target of a vertex is its position in the cheapest order found,
+  divided by n - 1; the batched path orders by lowest score among the
+  frontier, so a network that fits the targets reproduces that order;
+* at serving time a learned-order query that exceeds its work limit is run
+  again with the heuristic order, so counts never depend on the network.
+"""
+from __future__ import annotations
+
+import dataclasses
+from pathlib import Path
+from typing import Sequence
+
+import numpy as np
+
+from . import (ALGO_FUSED, ELIMIT, ORDER_GIVEN, ORDER_HEURISTIC, ORDER_LEARNED, Engine, Query,
+               mpnn_param_count)
+
+F_IN, F_PAD, H, LAYERS = 8, 16, 64, 3
+P_WIN = 0
+P_BIN = P_WIN + F_PAD * H
+P_WS = P_BIN + H
+P_WN = P_WS + LAYERS * H * H
+P_B = P_WN + LAYERS * H * H
+P_WOUT = P_B + LAYERS * H
+P_BOUT = P_WOUT + H
+N_PARAMS = P_BOUT + 1
+
+WEIGHTS = Path(__file__).resolve().parent / "order_net.npy"
+UNCAPPED = 1 << 60  # a work limit that only turns on counting
+
+
+def init_params(seed: int = 0) -> np.ndarray:
+    """He-normal weights, zero biases; the padding rows of W_in stay zero."""
+    assert N_PARAMS == mpnn_param_count()
+    rng = np.random.default_rng(seed)
+    p = np.zeros(N_PARAMS, np.float32)
+    w_in = np.zeros((F_PAD, H), np.float32)
+    w_in[:F_IN] = rng.normal(0, np.sqrt(2.0 / F_IN), (F_IN, H))
+    p[P_WIN:P_BIN] = w_in.reshape(-1)
+    p[P_WS:P_WN] = rng.normal(0, np.sqrt(1.0 / H), LAYERS * H * H)
+    p[P_WN:P_B] = rng.normal(0, np.sqrt(1.0 / H), LAYERS * H * H)
+    p[P_WOUT:P_BOUT] = rng.normal(0, np.sqrt(1.0 / H), H)
+    p[P_BOUT] = 0.5
+    return p
+
+
+def load_params(path=None) -> np.ndarray:
+    p = np.load(path or WEIGHTS).astype(np.float32)
+    if p.size != N_PARAMS:
+        raise ValueError(f"{path}: {p.size} parameters, expected {N_PARAMS}")
+    return p
+
+
+def adjacency_masks(q: Query) -> np.ndarray:
+    m = np.zeros(q.num_vertices, np.uint32)
+    for a, b in np.asarray(q.edges).reshape(-1, 2).tolist():
+        if a != b:
+            m[a] |= np.uint32(1 << b)
+            m[b] |= np.uint32(1 << a)
+    return m
+
+
+def is_connected_order(order, masks) -> bool:
+    placed = 0
+    for i, u in enumerate(order):
+        if i and not (int(masks[u]) & placed):
+            return False
+        placed |= 1 << int(u)
+    return True
+
+
+def local_moves(order, masks, k: int, rng: np.random.Generator) -> list:
+    """Up to k distinct connected orders one move away from `order`: a vertex
+    taken from position i and inserted at an earlier position j."""
+    n = len(order)
+    out, seen = [], {tuple(order)}
+    for _ in range(16 * k):
+        if len(out) >= k or n < 2:
+            break
+        i = int(rng.integers(1, n))
+        j = int(rng.integers(0, i))
+        o = list(order[:j]) + [order[i]] + list(order[j:i]) + list(order[i + 1:])
+        t = tuple(o)
+        if t not in seen and is_connected_order(o, masks):
+            seen.add(t)
+            out.append(o)
+    return out
+
+
+def alternative_orders(q: Query, cand, k: int, rng: np.random.Generator, around=None) -> list:
+    """Up to k distinct connected orders: half are single moves from `around`
+    (the heuristic order) when given; the rest greedy by candidate count
+    divided by (1 + alpha * placed neighbours), with multiplicative log-normal
+    noise of several strengths, and uniformly random frontier walks."""
+    n = q.num_vertices
+    masks = [int(x) for x in adjacency_masks(q)]
+    cnt = np.maximum(np.asarray(cand, np.float64), 1.0)
+    out = local_moves(list(around), masks, k // 2, rng) if around is not None else []
+    seen = {tuple(o) for o in out}
+    if around is not None:
+        seen.add(tuple(around))
+    tries = 0
+    while len(out) < k and tries < 8 * k:
+        tries += 1
+        sigma = (0.25, 0.75, 1.5, None)[tries % 4]
+        alpha = float(rng.choice([0.0, 0.5, 1.0, 2.0]))
+        noisy = rng.random(n) if sigma is None else cnt * np.exp(rng.normal(0, sigma, n))
+        placed, order = 0, []
+        for i in range(n):
+            best, bv = -1, np.inf
+            for u in range(n):
+                if (placed >> u) & 1 or (i and not (masks[u] & placed)):
+                    continue
+                back = bin(masks[u] & placed).count("1")
+                v = noisy[u] / (1.0 + alpha * back) if sigma is not None else noisy[u]
+                if v < bv:
+                    best, bv = u, v
+            order.append(best)
+            placed |= 1 << best
+        t = tuple(order)
+        if t not in seen:
+            seen.add(t)
+            out.append(list(order))
+    return out
+
+
+@dataclasses.dataclass
+class QueryLog:
+    query: Query
+    candidates: list        # post-filter candidate count per vertex
+    count: int
+    hash: int
+    heuristic_order: list
+    heuristic_work: int
+    orders: list            # alternatives that finished within the limit
+    works: list
+    level_counts: list      # per alternative
+    aborted: int            # alternatives stopped by the limit
+
+    @property
+    def best(self):
+        """The cheapest order found; the heuristic order unless an alternative
+        examined at least 2% fewer entries."""
+        if self.works and min(self.works) < 0.98 * self.heuristic_work:
+            i = int(np.argmin(self.works))
+            return self.orders[i], self.works[i]
+        return self.heuristic_order, self.heuristic_work
+
+
+def collect_logs(engine: Engine, queries: Sequence[Query], algo: int = ALGO_FUSED, per_query: int = 16,
+                 seed: int = 0, batch: int = 2048, heuristic_limit: int = 0) -> list:
+    """Order/cost logs for the queries on the engine's resident graph.
+    Queries whose heuristic run exceeds heuristic_limit (0: none) are dropped.
+    Alternatives run in batches that share one work limit, the largest
+    heuristic work among their queries; an alternative costlier than its own
+    query's heuristic is recorded as aborted."""
+    rng = np.random.default_rng(seed)
+    logs = []
+    limit = heuristic_limit or UNCAPPED
+    for s in range(0, len(queries), batch):
+        part = [Query(q.labels, q.edges) for q in queries[s:s + batch]]
+        res = engine.match_batch(part, algo=algo, order_source=ORDER_HEURISTIC, max_work=limit)
+        alts = []
+        for q, r in zip(part, res):
+            if r.status != 0:
+                continue
+            lg = QueryLog(q, list(r.candidates), r.count, r.hash, list(r.order), int(r.work), [], [], [], 0)
+            logs.append(lg)
+            for o in alternative_orders(q, r.candidates, per_query, rng, around=lg.heuristic_order):
+                alts.append((Query(q.labels, q.edges, order=np.asarray(o, np.uint32)), lg))
+        # sort by the owner's work so each batch's shared limit stays close to its members'
+        alts.sort(key=lambda t: t[1].heuristic_work)
+        for s2 in range(0, len(alts), batch):
+            items = alts[s2:s2 + batch]
+            lim = max(max(lg.heuristic_work for _, lg in items), 1)
+            rr = engine.match_batch([a for a, _ in items], algo=algo, order_source=ORDER_GIVEN, max_work=lim)
+            for (aq, lg), r in zip(items, rr):
+                if r.status == ELIMIT or (r.status == 0 and r.work > lg.heuristic_work):
+                    lg.aborted += 1
+                    continue
+                if r.status != 0:
+                    raise RuntimeError(f"alternative order failed with status {r.status}")
+                if r.count != lg.count or r.hash != lg.hash:
+                    raise RuntimeError("an alternative order changed the result")
+                lg.orders.append([int(x) for x in aq.order])
+                lg.works.append(int(r.work))
+                lg.level_counts.append(list(r.level_counts))
+    return logs
+
+
+def training_set(engine: Engine, logs: Sequence[QueryLog], algo: int = ALGO_FUSED):
+    """(node offsets, features, neighbour masks, targets) for the logs."""
+    qs = [lg.query for lg in logs]
+    feat = engine.mpnn_features(qs, [lg.candidates for lg in logs], algo)
+    goff = np.zeros(len(qs) + 1, np.uint32)
+    goff[1:] = np.cumsum([q.num_vertices for q in qs])
+    nbr = np.concatenate([adjacency_masks(q) for q in qs]) if qs else np.zeros(0, np.uint32)
+    tgt = np.zeros(int(goff[-1]), np.float32)
+    for i, lg in enumerate(logs):
+        order, _ = lg.best
+        n = len(order)
+        for pos, u in enumerate(order):
+            tgt[goff[i] + u] = pos / max(n - 1, 1)
+    return goff, feat, nbr, tgt
+
+
+def _subset(goff, feat, nbr, tgt, idx):
+    sizes = (goff[1:] - goff[:-1])[idx]
+    sel = np.concatenate([np.arange(goff[i], goff[i + 1]) for i in idx]) if len(idx) else np.zeros(0, np.int64)
+    off = np.zeros(len(idx) + 1, np.uint32)
+    off[1:] = np.cumsum(sizes)
+    return off, feat[sel], nbr[sel], tgt[sel]
+
+
+def train(engine: Engine, data, epochs: int = 60, lr: float = 2e-3, batch_graphs: int = 256, seed: int = 0,
+          params: np.ndarray | None = None, verbose: bool = False):
+    """Minibatch Adam on the device kernels.  Returns (params, mean loss per epoch)."""
+    goff, feat, nbr, tgt = data
+    engine.mpnn_set_params(init_params(seed) if params is None else params)
+    rng = np.random.default_rng(seed)
+    G = len(goff) - 1
+    losses = []
+    for ep in range(epochs):
+        perm = rng.permutation(G)
+        tot, nb = 0.0, 0
+        for s in range(0, G, batch_graphs):
+            loss, _ = engine.mpnn_train_step(*_subset(goff, feat, nbr, tgt, perm[s:s + batch_graphs]), lr=lr)
+            tot += loss
+            nb += 1
+        losses.append(tot / max(nb, 1))
+        if verbose:
+            print(f"epoch {ep} loss {losses[-1]:.5f}", flush=True)
+    return engine.mpnn_get_params(), losses
+
+
+def match_learned(engine: Engine, queries: Sequence[Query], algo: int = ALGO_FUSED, work_limit: int = 0, **kw):
+    """Batched learned-order matching with the heuristic order as fallback:
+    queries that exceed work_limit under the learned order run again with the
+    heuristic order (unlimited).  Returns (results, number of fallbacks)."""
+    res = engine.match_batch(queries, algo=algo, order_source=ORDER_LEARNED, max_work=work_limit, **kw)
+    redo = [i for i, r in enumerate(res) if r.status == ELIMIT]
+    if redo:
+        again = engine.match_batch([queries[i] for i in redo], algo=algo, order_source=ORDER_HEURISTIC, **kw)
+        for i, r in zip(redo, again):
+            res[i] = r
+    return res, len(redo)

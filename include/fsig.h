@@ -78,6 +78,7 @@ typedef struct {
   uint64_t level_counts[FSIG_MAX_QUERY];/* partial embeddings of length d+1, d=0..n-1   */
   float ms_filter;                      /* device time: filter + refinement            */
   float ms_join;                        /* device time: enumeration                    */
+  uint64_t work;                        /* driver entries examined (when max_work set)  */
 } fsig_result;
 
 typedef struct {
@@ -116,6 +117,16 @@ int fsig_load_graph_file(fsig_engine* e, const char* path, int is_labeled);
 int fsig_graph_info(const fsig_engine* e, uint32_t* num_vertices, uint64_t* num_adj,
                     int32_t* num_labels, uint32_t* max_degree);
 
+/* ---- host reader; replaces UndirectedSurveyPlainReader::read (IO/graph_reader.cc:12-55)
+ *      for callers that want the parsed graph itself (query files, the CLI).
+ *      The handle owns labels[num_vertices] (-1 for ids without a v record) and
+ *      edges[2 * num_edges] (file order, duplicates kept). ---- */
+typedef struct fsig_graph_file fsig_graph_file;
+int fsig_read_graph_file(const char* path, int is_labeled, fsig_graph_file** out);
+int fsig_graph_file_data(const fsig_graph_file* f, uint32_t* num_vertices, const int32_t** labels,
+                         uint64_t* num_edges, const uint32_t** edges);
+void fsig_free_graph_file(fsig_graph_file* f);
+
 /* ---- matching; replaces GPUSubgraphMatcher::match (match/subgraph_match.h:46),
  *      i.e. MMatch::match (match/MMatch.cu:2077-2121, algo 1) and GSI::match
  *      (match/GSI.cu:329-358, algo 2), for one query. ---- */
@@ -123,6 +134,48 @@ int fsig_match(fsig_engine* e, const fsig_query* q, int algo, fsig_result* out);
 /* Many queries against the resident data graph in one persistent launch. */
 int fsig_match_batch(fsig_engine* e, uint32_t num_queries, const fsig_query* qs,
                      const fsig_batch_opts* opts, fsig_result* out);
+
+/* ---- embeddings; the output the reference's EmbeddingWriter::write
+ *      (IO/embedding_writer.h:12-20, an empty stub there) was meant to produce.
+ *      sink receives rows[num_rows * width]: one embedding per row, column u =
+ *      the data vertex (caller id) matched to query vertex u.  Rows come in
+ *      chunks of at most buffer_rows (0: 2^20); a non-zero return stops.  When
+ *      a query has more embeddings than one buffer holds, its root tasks are
+ *      cut into ranges matched one after the other.  out gets the count and
+ *      hash of the whole set, as fsig_match. ---- */
+typedef int (*fsig_embedding_sink)(void* user, const uint32_t* rows, uint64_t num_rows, uint32_t width);
+int fsig_match_embeddings(fsig_engine* e, const fsig_query* q, int algo, uint64_t buffer_rows,
+                          fsig_embedding_sink sink, void* user, fsig_result* out);
+/* PlainEmbeddingWriter: the embeddings as text, one per line, the data ids of
+ * query vertices 0..n-1 separated by spaces. */
+int fsig_write_embeddings(fsig_engine* e, const fsig_query* q, int algo, const char* path, fsig_result* out);
+
+/* ---- order-scoring network (no counterpart in the reference, which orders by
+ *      the heuristics of match/GSI.cu:105-149 and match/MMatch.cu:1575-1641).
+ *      A 3-layer message-passing network over the query graph, hidden 64, BF16
+ *      weights and activations with FP32 accumulation, scoring each query
+ *      vertex from 8 features; FSIG_ORDER_LEARNED orders by lowest score among
+ *      the frontier.  Graphs are passed as node offsets (graph g has nodes
+ *      [node_offsets[g], node_offsets[g+1]), at most 32), 8 features per node
+ *      and a neighbour bitmask per node (local ids).  Parameters are FP32, in
+ *      the layout documented in fsig_gb300/csrc/mpnn.h. ---- */
+uint32_t fsig_mpnn_param_count(void);
+int fsig_mpnn_set_params(fsig_engine* e, const float* params, uint32_t count);
+int fsig_mpnn_get_params(fsig_engine* e, float* params, uint32_t count);
+/* Features of each query vertex given its candidate count (candidates[] in
+ * query order, vertex order), computed on the device as the batched path does:
+ * position in algo's heuristic order/(n-1), degree/8, plog2(candidates)/20,
+ * plog2(label class size)/20, candidates/class size, signature bits/16, n/32,
+ * mean plog2 of neighbours' candidates/20, where plog2(x) = e + x/2^e - 1,
+ * e = floor(log2 x).  features[8 * total vertices]. */
+int fsig_mpnn_features(fsig_engine* e, uint32_t num_queries, const fsig_query* qs, int algo,
+                       const uint32_t* candidates, float* features);
+int fsig_mpnn_forward(fsig_engine* e, uint32_t num_graphs, const uint32_t* node_offsets, const float* features,
+                      const uint32_t* neighbours, float* scores);
+/* One training step on the mean squared error against targets: loss, the
+ * gradients (grads may be NULL) and, when lr > 0, an Adam update. */
+int fsig_mpnn_train_step(fsig_engine* e, uint32_t num_graphs, const uint32_t* node_offsets, const float* features,
+                         const uint32_t* neighbours, const float* targets, float lr, float* loss, float* grads);
 
 /* ---- statistics of the engine's last fsig_match / fsig_match_batch call ----
  * (no reference counterpart: the reference prints phase timings with its
