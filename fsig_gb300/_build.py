@@ -2,6 +2,7 @@
 
 libfsig.so      the CUDA engine (sm_103a only) behind include/fsig.h
 libfsig_gen.so  the host workload generators behind include/fsig_gen.h
+FSIG            the command line (csrc/cli.cpp) on libfsig.so
 
 Translation units are compiled in parallel; objects and libraries go to
 fsig_gb300/_build/.  A library is rebuilt when any of its sources or headers
@@ -87,11 +88,24 @@ def build_gen(force: bool = False) -> Path:
     return lib
 
 
+def build_cli(force: bool = False) -> Path:
+    """The FSIG executable, linked against the in-tree libfsig.so."""
+    OUT.mkdir(exist_ok=True)
+    exe = OUT / "FSIG"
+    src = CSRC / "cli.cpp"
+    lib = OUT / "libfsig.so"
+    if force or _stale(exe, [src, lib, INCLUDE / "fsig.h"]):
+        _run(["g++", "-O2", "-std=c++17", "-Wall", "-I", str(INCLUDE), "-o", str(exe), str(src), "-L", str(OUT),
+              "-lfsig", "-Wl,-rpath,$ORIGIN"])
+    return exe
+
+
 def build_all(force: bool = False) -> None:
     with cf.ThreadPoolExecutor(max_workers=2) as ex:
         futs = [ex.submit(build_engine, force), ex.submit(build_gen, force)]
         for f in futs:
             f.result()
+    build_cli(force)
 
 
 if __name__ == "__main__":
