@@ -844,9 +844,17 @@ int run_embeddings(Engine& e, const HostQuery& q, BatchOptions opt, uint64_t buf
   }
   // More embeddings than one buffer holds: cut the task space into ranges,
   // matched one after the other, halving a range whose rows still overflow.
+  // Tasks are made as small as they go (32 depth-1 entries) so that a range
+  // of one task is unlikely to overflow; an empty range gives their number.
   first.rows.clear();
   const uint64_t total = first.res[0].count;
-  const uint32_t T = first.tasks_total;
+  opt.split = 32;
+  opt.task_begin = 0;
+  opt.task_end = 0;
+  BatchOutput probe;
+  rc = run_batch(e, qs, opt, probe);
+  if (rc) return rc;
+  const uint32_t T = probe.tasks_total;
   const uint64_t parts = std::max<uint64_t>(1, std::min<uint64_t>(T, 2 * ((total + buffer_rows - 1) / buffer_rows)));
   std::vector<std::pair<uint32_t, uint32_t>> todo;
   for (uint64_t i = parts; i-- > 0;) todo.push_back({uint32_t(T * i / parts), uint32_t(T * (i + 1) / parts)});

@@ -260,3 +260,76 @@ def match_learned(engine: Engine, queries: Sequence[Query], algo: int = ALGO_FUS
         for i, r in zip(redo, again):
             res[i] = r
     return res, len(redo)
+
+
+# ---------------------------------------------------------------------------
+# training the packaged network: logs on the mid-scale graphs
+# ---------------------------------------------------------------------------
+def training_workloads():
+    """(name, graph builder, query specs) of the logs the packaged network is
+    trained on: the 320k-vertex Chung-Lu graph (exponent 2.1, seed 2, 16 Zipf
+    labels) with 8-vertex and 4-32-vertex dense and sparse random-walk queries,
+    and the unlabeled 2^20-vertex R-MAT graph (seed 3, 2^24 edges) with
+    5-vertex queries.  Query seeds start at 70,000,000, apart from the ones the
+    benchmark draws."""
+    from . import QUERY_DENSE, QUERY_INDUCED, QUERY_SPARSE, gen_chung_lu, gen_labels, gen_rmat
+
+    def chung_lu():
+        lab = gen_labels(320000, 16, "zipf", seed=2)
+        return gen_chung_lu(320000, 1050000, 2.1, seed=2, labels=lab)
+
+    def rmat():
+        return gen_rmat(1 << 20, 1 << 24, 0.57, 0.19, 0.19, seed=3)
+
+    rng = np.random.default_rng(70)
+    mixed = [(int(n), QUERY_DENSE if i % 2 else QUERY_SPARSE, 70_000_000 + i, 4)
+             for i, n in enumerate(rng.integers(4, 33, 3000))]
+    eight = [(8, QUERY_DENSE if i % 2 else QUERY_SPARSE, 71_000_000 + i, 4) for i in range(600)]
+    five = [(5, QUERY_INDUCED, 72_000_000 + i) for i in range(300)]
+    return [("chung-lu 320k", chung_lu, mixed + eight), ("r-mat 2^20 unlabeled", rmat, five)]
+
+
+def main(argv=None):
+    import argparse
+    import time
+
+    from . import gen_queries, select_within_budget
+    ap = argparse.ArgumentParser(description="Train the order-scoring network on the engine's own logs.")
+    ap.add_argument("--out", default=str(WEIGHTS))
+    ap.add_argument("--per-query", type=int, default=16)
+    ap.add_argument("--epochs", type=int, default=60)
+    ap.add_argument("--lr", type=float, default=2e-3)
+    ap.add_argument("--work-limit", type=int, default=1 << 24, help="drop queries whose heuristic run examines more")
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--device", type=int, default=0)
+    args = ap.parse_args(argv)
+    logs = []
+    with Engine(args.device, arena_bytes=48 << 30) as e:
+        t0 = time.time()
+        for name, build, specs in training_workloads():
+            g = build()
+            csr = g.csr()
+            e.load_graph(g)
+            qs = select_within_budget(e, gen_queries(g, specs, csr=csr), len(specs), args.work_limit)
+            lg = collect_logs(e, qs, per_query=args.per_query, seed=args.seed)
+            gain = sum(x.heuristic_work for x in lg) / max(sum(x.best[1] for x in lg), 1)
+            print(f"[learn] {name}: {len(lg)} queries logged, best/heuristic total work 1/{gain:.3f}, "
+                  f"{time.time() - t0:.1f}s", flush=True)
+            logs.append((lg, training_set(e, lg)))
+        goff = np.zeros(1, np.uint32)
+        feats, nbrs, tgts = [], [], []
+        for _, (o, f, nb, t) in logs:
+            goff = np.concatenate([goff, goff[-1] + o[1:]])
+            feats.append(f)
+            nbrs.append(nb)
+            tgts.append(t)
+        data = (goff, np.concatenate(feats), np.concatenate(nbrs), np.concatenate(tgts))
+        params, losses = train(e, data, epochs=args.epochs, lr=args.lr, seed=args.seed)
+        print(f"[learn] trained {len(goff) - 1} graphs, loss {losses[0]:.4f} -> {losses[-1]:.4f}, "
+              f"{time.time() - t0:.1f}s", flush=True)
+        np.save(args.out, params)
+        print(f"[learn] wrote {args.out}", flush=True)
+
+
+if __name__ == "__main__":
+    main()
