@@ -13,6 +13,14 @@ compaction + enumeration.
           wall time including packing, host->device copies of the query
           descriptors and device->host copies of the results
 
+Order: the learned order (the packaged order-scoring network,
+fsig_gb300/order_net.npy, trained on logs of the mid-scale graphs) when it
+exists, with a per-query work limit; a query over the limit runs again in the
+heuristic order, inside the timed region.  After the timed region the same
+batches run in heuristic order ("heuristic_batched"), and every count and
+hash is compared between the two.  "single_query_path" is the plain
+one-query-per-call heuristic path (fsig_match) on a sample.
+
 Workloads (synthetic, seeded; no dataset is available):
   c5  Chung-Lu 2^22 vertices / 2^26 edges, exponent 2.0, seed 5, 32 Zipf
       labels; 2048 queries of 12-32 vertices, batches of 512 (default)
@@ -256,45 +264,94 @@ def cpu_sample(g, csr, queries, budget_s):
 # ---------------------------------------------------------------------------
 # arms
 # ---------------------------------------------------------------------------
+class StepStats:
+    """Device time and traffic of the engine calls one arm makes."""
+
+    def __init__(self):
+        self.dev_ms = self.enum_ms = 0.0
+        self.enum_bytes = self.launches = self.h2d = self.d2h = self.passes = 0
+
+    def add(self, st):
+        self.dev_ms += st["ms_filter"] + st["ms_join"]
+        self.enum_ms += st["ms_enum"]
+        self.enum_bytes += st["enum_bytes"]
+        self.launches += st["kernel_launches"]
+        self.passes += st["enum_passes"]
+        self.h2d += st["h2d_bytes"]
+        self.d2h += st["d2h_bytes"]
+
+
+def learned_step(e, b, algo, limit, acc):
+    """One batch in learned order; queries over the work limit run again in
+    heuristic order (the fallback).  Returns (results, fallbacks)."""
+    rs = e.match_batch(b, algo=algo, order_source=F.ORDER_LEARNED, max_work=limit)
+    acc.add(e.last_stats())
+    redo = [i for i, r in enumerate(rs) if r.status == F.ELIMIT]
+    if redo:
+        again = e.match_batch([b[i] for i in redo], algo=algo, order_source=F.ORDER_HEURISTIC)
+        acc.add(e.last_stats())
+        for i, r in zip(redo, again):
+            rs[i] = r
+    return rs, len(redo)
+
+
 def run_ours(args, dist):
+    from fsig_gb300 import learn
     dev = dist.local
     algo = {"fsig": F.ALGO_FSIG, "gsi": F.ALGO_GSI, "fused": F.ALGO_FUSED}[args.algo]
-    order = {"heuristic": F.ORDER_HEURISTIC, "learned": F.ORDER_LEARNED}[args.order]
+    order = args.order or ("learned" if learn.WEIGHTS.exists() else "heuristic")
     with F.Engine(dev, arena_bytes=args.arena_gb << 30) as e:
         g, csr, gdesc, batches = make_workload(args.workload, dist.rank, e)
         info = e.graph_info()
         log(f"[bench] graph resident: {info}")
-        kw = dict(algo=algo, order_source=order, max_work=args.max_work)
+        if order == "learned":
+            e.mpnn_set_params(learn.load_params())
+        limit = args.max_work or (WORK_BUDGET if order == "learned" else 0)
+
+        def step(b, acc):
+            if order == "learned":
+                return learned_step(e, b, algo, limit, acc)
+            rs = e.match_batch(b, algo=algo, order_source=F.ORDER_HEURISTIC, max_work=limit)
+            acc.add(e.last_stats())
+            return rs, 0
+
         for i in range(args.warmup):
-            e.match_batch(batches[i % len(batches)], **kw)
+            step(batches[i % len(batches)], StepStats())
         dist.barrier()
         cuda_sync()
-        dev_ms = enum_ms = 0.0
-        nq = emb = enum_bytes = launches = h2d = d2h = passes = over = 0
+        acc = StepStats()
+        nq = emb = over = fallbacks = 0
+        results = []
         with ClockSampler(dev) as clk:
             t0 = time.perf_counter()
             for k in range(args.steps):
                 b = batches[k % len(batches)]
-                rs = e.match_batch(b, **kw)
-                st = e.last_stats()
-                dev_ms += st["ms_filter"] + st["ms_join"]
-                enum_ms += st["ms_enum"]
-                enum_bytes += st["enum_bytes"]
-                launches += st["kernel_launches"]
-                passes += st["enum_passes"]
-                h2d += st["h2d_bytes"]
-                d2h += st["d2h_bytes"]
+                before = acc.dev_ms
+                rs, fb = step(b, acc)
+                results.append([(r.count, r.hash) for r in rs])
                 nq += len(b)
                 emb += sum(r.count for r in rs)
                 over += sum(1 for r in rs if r.status == F.ELIMIT)
-                log(f"[bench] step {k}: {len(b)} queries, {sum(r.count for r in rs)} embeddings, filter "
+                fallbacks += fb
+                st = e.last_stats()
+                log(f"[bench] step {k}: {len(b)} queries, {sum(r.count for r in rs)} embeddings, device "
+                    f"{acc.dev_ms - before:.2f} ms ({order} order, {fb} fallbacks); last call: filter "
                     f"{st['ms_filter']:.2f} ms, join {st['ms_join']:.2f} ms (enumeration {st['ms_enum']:.2f} ms, "
-                    f"{st['enum_passes']} passes), over limit {sum(1 for r in rs if r.status == F.ELIMIT)}; "
-                    f"tasks {st['enum_tasks']} pops {st['enum_pops']} handoffs {st['enum_handoffs']} "
-                    f"records {st['enum_records']} examines {st['enum_examines']}")
+                    f"{st['enum_passes']} passes); tasks {st['enum_tasks']} pops {st['enum_pops']} handoffs "
+                    f"{st['enum_handoffs']} records {st['enum_records']} examines {st['enum_examines']}")
             cuda_sync()
             wall = time.perf_counter() - t0
         dist.barrier()
+        # the same batches in heuristic order: the comparison and the bit-exactness check
+        heur = StepStats()
+        identical = True
+        for k in range(args.steps):
+            b = batches[k % len(batches)]
+            rs = e.match_batch(b, algo=algo, order_source=F.ORDER_HEURISTIC)
+            heur.add(e.last_stats())
+            identical &= [(r.count, r.hash) for r in rs] == results[k]
+        dev_ms, enum_ms, enum_bytes = acc.dev_ms, acc.enum_ms, acc.enum_bytes
+        launches, h2d, d2h, passes = acc.launches, acc.h2d, acc.d2h, acc.passes
         # the plain single-query path (fsig_match, heuristic order) on a sample
         single = batches[0][: args.single_sample]
         t1 = time.perf_counter()
@@ -302,6 +359,7 @@ def run_ours(args, dist):
             e.match(q, F.ALGO_GSI)
         single_qps = len(single) / (time.perf_counter() - t1)
     clocks = clk.summary()
+    heur_s = dist.max(heur.dev_ms / 1e3)
     dev_s = dist.max(dev_ms / 1e3)
     wall_s = dist.max(wall)
     tot_q = dist.sum(nq)
@@ -325,14 +383,18 @@ def run_ours(args, dist):
         "dtype": "u32",
         "data": "synthetic (seeded generators; no dataset available)",
         "config": {"workload": args.workload, "graph": gdesc, "queries_per_step": len(batches[0]),
-                   "algo": args.algo, "order": args.order, "parallelism": f"replicas x{dist.world}, queries sharded",
+                   "algo": args.algo, "order": order, "parallelism": f"replicas x{dist.world}, queries sharded",
                    "l2": "inputs larger than L2 (resident graph arrays > 129 MB)" if args.workload in ("c5",) else
                    "graph fits L2; batches differ step to step",
-                   "max_work": args.max_work, "queries_over_limit": over,
+                   "work_limit": limit, "queries_over_limit": over, "learned_fallbacks": fallbacks,
                    "selection": f"first queries of a seeded random-walk sequence whose enumeration examines at most "
                                 f"{WORK_BUDGET} driver entries"},
         "e2e": {"value": round(tot_q / wall_s, 3), "unit": "queries/s",
                 "h2d_bytes_per_step": int(h2d / args.steps), "d2h_bytes_per_step": int(d2h / args.steps)},
+        "heuristic_batched": {"value": round(tot_q / heur_s, 3), "unit": "queries/s",
+                              "ms_per_step": round(heur_s * 1e3 / args.steps, 3),
+                              "counts_and_hashes_identical": bool(identical),
+                              "note": "the same batches in heuristic order, device time, after the timed region"},
         "single_query_path": {"value": round(single_qps, 3), "unit": "queries/s",
                               "sample": f"first {len(single)} queries of batch 0, one fsig_match call each (algo 2, "
                                         "reference-exact heuristic order), wall clock"},
@@ -403,8 +465,10 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", default="c5", choices=["c5", "c4", "c2", "c1"])
     ap.add_argument("--algo", default="fused", choices=["fsig", "gsi", "fused"])
-    ap.add_argument("--order", default="heuristic", choices=["heuristic", "learned"])
-    ap.add_argument("--max-work", type=int, default=0)
+    ap.add_argument("--order", default=None, choices=["heuristic", "learned"],
+                    help="default: learned when the packaged network exists")
+    ap.add_argument("--max-work", type=int, default=0,
+                    help="per-query work limit (default: the selection budget in learned order, none otherwise)")
     ap.add_argument("--arena-gb", type=int, default=64)
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--ref-step-s", type=float, default=8.0)

@@ -61,7 +61,7 @@ class _BatchOpts(C.Structure):
 class _Stats(C.Structure):
     _fields_ = [("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64), ("enum_bytes", C.c_uint64),
                 ("kernel_launches", C.c_uint32), ("enum_passes", C.c_uint32), ("ms_filter", C.c_float),
-                ("ms_join", C.c_float), ("ms_enum", C.c_float), ("pad", C.c_float), ("enum_tasks", C.c_uint64),
+                ("ms_join", C.c_float), ("ms_enum", C.c_float), ("graph", C.c_uint32), ("enum_tasks", C.c_uint64),
                 ("enum_pops", C.c_uint64), ("enum_handoffs", C.c_uint64), ("enum_records", C.c_uint64),
                 ("enum_examines", C.c_uint64)]
 
@@ -433,7 +433,7 @@ class Engine:
     def last_stats(self) -> dict:
         st = _Stats()
         self._check(self._L.fsig_last_stats(self._h, C.byref(st)), "last_stats")
-        return {k: getattr(st, k) for k, _ in _Stats._fields_ if k != "pad"}
+        return {k: getattr(st, k) for k, _ in _Stats._fields_}
 
     # transforms and filter probe
     def build_csr(self, V: int, edges: np.ndarray):

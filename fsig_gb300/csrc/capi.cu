@@ -170,6 +170,7 @@ int fsig_destroy(fsig_engine* h) {
   for (auto& ev : h->e.ev_enum)
     if (ev) cudaEventDestroy(ev);
   fsig::mpnn_free(h->e);
+  if (h->e.gexec) cudaGraphExecDestroy(h->e.gexec);
   if (h->e.arena.base) cudaFree(h->e.arena.base);
   if (h->e.pinned) cudaFreeHost(h->e.pinned);
   if (h->e.stream) cudaStreamDestroy(h->e.stream);
@@ -350,6 +351,7 @@ int fsig_match_batch(fsig_engine* h, uint32_t nq, const fsig_query* qs, const fs
     if (!h->e.mpnn || !h->e.mpnn->loaded) return finish(h, fsig::fail(FSIG_EINVAL, "no order network loaded"));
     o.learned = true;
   }
+  o.use_graph = bo.use_graph != 0;
   if (bo.chunk) o.chunk = bo.chunk;
   if (bo.split_len) o.split = bo.split_len;
   if (bo.split_cycles) o.budget_cycles = (long long)bo.split_cycles;

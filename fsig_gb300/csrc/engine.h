@@ -54,6 +54,8 @@ struct Engine {
   uint64_t cur_h2d = 0;  // host-to-device bytes of the call in progress
   unsigned long long last_ev[8] = {0};  // enumeration event counters of the last call
   struct MpnnState* mpnn = nullptr;      // order-scoring network (mpnn.cu), created on first use
+  bool mpnn_configured = false;          // its kernels' shared-memory attributes are set
+  cudaGraphExec_t gexec = nullptr;       // the last batch's executable graph, updated in place
 };
 
 // graph_store.cu

@@ -49,7 +49,7 @@ struct EnumArgs {
   const uint32_t* __restrict__ roots;
   const uint32_t* __restrict__ root_q;
   const uint32_t* __restrict__ chunk_off;  // [nroots + 1]
-  uint32_t nroots;
+  const uint32_t* __restrict__ nroots_ptr;  // number of roots (device)
   uint32_t split;
   uint32_t t_end;  // pass-0 tasks [initial ctr[0], t_end) (a range of the task space)
   // explicit input tasks (passes >= 1)
@@ -131,7 +131,8 @@ __global__ void __launch_bounds__(256) enumerate_kernel(EnumArgs A) {
   const uint32_t lane = threadIdx.x & 31;
   const GraphView& g = A.g;
   const uint64_t W1 = uint64_t(g.L) + 1;
-  const uint32_t T_in = A.in_tasks ? A.in_count : min(A.chunk_off[A.nroots], A.t_end);
+  const uint32_t nroots = A.in_tasks ? 0u : *A.nroots_ptr;
+  const uint32_t T_in = A.in_tasks ? A.in_count : min(A.chunk_off[nroots], A.t_end);
 
   // lane-distributed level state
   uint32_t f = 0, dpos = 0, dend = 0, drv = 0, cnt = 0, it = 0;
@@ -292,10 +293,11 @@ __global__ void __launch_bounds__(256) enumerate_kernel(EnumArgs A) {
   // depth done here.  Returns false when the queue has no room.
   auto donate = [&](uint32_t d0, uint32_t lv) -> bool {
     const uint32_t n = ws.plan.n;
+    const uint32_t hand = max(A.split, 32u);  // driver entries per handed-off range
     uint32_t mine = 0;
     if (lane >= d0 && lane <= lv) {
       if (lane + 1 < n && cnt > it) mine += cnt - it;
-      if (dend > dpos) mine += (dend - dpos + A.split - 1) / A.split;
+      if (dend > dpos) mine += (dend - dpos + hand - 1) / hand;
     }
     const uint32_t has = __ballot_sync(kFull, mine > 0);
     if (!has) return true;
@@ -325,10 +327,10 @@ __global__ void __launch_bounds__(256) enumerate_kernel(EnumArgs A) {
         if (lane == 0) { r->q = cur_q; r->d = l + 1; r->lo = kInvalid; r->hi = kInvalid; }
       }
     }
-    for (uint32_t p = p_l; p < e_l; p += A.split) {
+    for (uint32_t p = p_l; p < e_l; p += hand) {
       TaskRec* r = A.out_tasks + slot++;
       if (lane < l) r->f[lane] = f;
-      if (lane == 0) { r->q = cur_q; r->d = l; r->lo = p; r->hi = min(p + A.split, e_l); }
+      if (lane == 0) { r->q = cur_q; r->d = l; r->lo = p; r->hi = min(p + hand, e_l); }
     }
     if (lane == l) {
       it = cnt;
@@ -505,7 +507,7 @@ __global__ void __launch_bounds__(256) enumerate_kernel(EnumArgs A) {
           run_record(A.in_tasks + t);
         } else {
           // implicit: root i, chunk c of its depth-1 driver range
-          uint32_t lo = 0, hi = A.nroots;  // last i with chunk_off[i] <= t
+          uint32_t lo = 0, hi = nroots;  // last i with chunk_off[i] <= t
           while (hi - lo > 1) {
             const uint32_t mid = (lo + hi) >> 1;
             if (A.chunk_off[mid] <= t) lo = mid; else hi = mid;

@@ -540,34 +540,64 @@ int filter_stage(Engine& e, const BatchLayout& b, uint32_t mode, int refine_iter
 namespace {
 constexpr uint32_t kOverflowCap = 1u << 20;  // task records per overflow queue
 
-// Runs the enumeration kernel over pass-0 tasks, then over the records each
-// pass leaves in its overflow queue, until none are left.
-int enumerate_passes(Engine& e, const BatchOptions& opt, const GraphView& gv, const Plan* d_plans,
-                     const uint32_t* pool, uint32_t Q, const uint32_t* d_roots, const uint32_t* d_root_q,
-                     const uint32_t* d_chunk_off, uint32_t nroots, uint32_t split, QueryResult* d_res,
-                     unsigned long long* d_misc, uint32_t* d_emit, unsigned long long* d_emit_ctr,
-                     uint32_t& passes, float& ms_enum, uint64_t& d2h) {
+__global__ void ctr_init_kernel(uint32_t* ctr, uint32_t first_task, uint32_t active) {
+  for (uint32_t i = threadIdx.x; i < 8 * kCtrStride; i += blockDim.x)
+    ctr[i] = i == 0 ? first_task : (i == 5 * kCtrStride ? active : 0u);
+}
+
+// The enumeration passes of one batch: pass 0 over the implicit root tasks,
+// then passes over the records each pass leaves in its overflow queue, until
+// none are left.  Launching a pass is stream-ordered work only (capturable);
+// deciding whether another pass is needed reads the counters the pass copied
+// to pinned host memory, after the stream has reached them.
+struct EnumRun {
+  EnumArgs A;
+  TaskRec *out = nullptr, *other = nullptr;
+  uint32_t *ready = nullptr, *other_ready = nullptr, *ctr = nullptr;
+  unsigned long long* d_ev = nullptr;
+  uint32_t* h_ctr = nullptr;  // pinned, 4 counters kCtrStride apart
+  uint32_t grid = 0, block = 0, active = 0, first_task = 0, pass = 0;
+  size_t smem = 0;
+};
+
+// One-time kernel attributes and occupancy (host calls, kept out of captures).
+int enum_configure(Engine& e) {
+  if (e.enum_per_sm) return FSIG_OK;
+  FSIG_CUDA_TRY(cudaFuncSetAttribute(enumerate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     int(sizeof(WarpSmem) * 8)));
+  int per = 0;
+  FSIG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, enumerate_kernel, 8 * 32, sizeof(WarpSmem) * 8));
+  e.enum_per_sm = std::max(per, 1);
+  return FSIG_OK;
+}
+
+int enum_prepare(Engine& e, const BatchOptions& opt, const GraphView& gv, const Plan* d_plans, const uint32_t* pool,
+                 uint32_t Q, const uint32_t* d_roots, const uint32_t* d_root_q, const uint32_t* d_chunk_off,
+                 const uint32_t* d_nroots, uint32_t split, QueryResult* d_res, unsigned long long* d_misc,
+                 uint32_t* d_emit, unsigned long long* d_emit_ctr, uint32_t* h_ctr, EnumRun& R) {
   cudaStream_t s = e.stream;
   TaskRec* qa = e.arena.take<TaskRec>(kOverflowCap);
   TaskRec* qb = e.arena.take<TaskRec>(kOverflowCap);
   uint32_t* ra = e.arena.take<uint32_t>(kOverflowCap);
   uint32_t* rb = e.arena.take<uint32_t>(kOverflowCap);
-  uint32_t* ctr = e.arena.take<uint32_t>(8 * kCtrStride);
-  if (!qa || !qb || !ra || !rb || !ctr) return fail(FSIG_EADMISSION, "work queues do not fit the device arena");
+  R.ctr = e.arena.take<uint32_t>(8 * kCtrStride);
+  R.d_ev = e.arena.take<unsigned long long>(8);
+  if (!qa || !qb || !ra || !rb || !R.ctr || !R.d_ev)
+    return fail(FSIG_EADMISSION, "work queues do not fit the device arena");
   FSIG_CUDA_TRY(cudaMemsetAsync(ra, 0, sizeof(uint32_t) * kOverflowCap, s));
   FSIG_CUDA_TRY(cudaMemsetAsync(rb, 0, sizeof(uint32_t) * kOverflowCap, s));
+  FSIG_CUDA_TRY(cudaMemsetAsync(R.d_ev, 0, 64, s));
+  FSIG_CUDA_TRY(cudaMemsetAsync(d_misc + 1, 0, sizeof(unsigned long long), s));
   const uint32_t wpb = std::max<uint32_t>(1, std::min<uint32_t>(opt.warps_per_block, 8));
-  const size_t smem = sizeof(WarpSmem) * wpb;
-  if (e.enum_per_sm == 0) {
-    FSIG_CUDA_TRY(cudaFuncSetAttribute(enumerate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       int(sizeof(WarpSmem) * 8)));
-    int per = 0;
-    FSIG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, enumerate_kernel, 8 * 32,
-                                                                sizeof(WarpSmem) * 8));
-    e.enum_per_sm = std::max(per, 1);
-  }
   const int per_sm = wpb == 8 ? e.enum_per_sm : std::max(1, e.enum_per_sm * 8 / int(wpb));
-  EnumArgs A;
+  R.smem = sizeof(WarpSmem) * wpb;
+  R.grid = uint32_t(e.num_sms * per_sm);
+  R.block = wpb * 32;
+  R.active = R.grid * wpb;  // every warp starts active; idle warps are counted as they wait
+  R.first_task = opt.task_begin;
+  R.h_ctr = h_ctr;
+  R.pass = 0;
+  EnumArgs& A = R.A;
   A.g = gv;
   A.plans = d_plans;
   A.pool = pool;
@@ -575,7 +605,7 @@ int enumerate_passes(Engine& e, const BatchOptions& opt, const GraphView& gv, co
   A.roots = d_roots;
   A.root_q = d_root_q;
   A.chunk_off = d_chunk_off;
-  A.nroots = nroots;
+  A.nroots_ptr = d_nroots;
   A.split = split;
   A.t_end = opt.task_end;
   A.emit = d_emit;
@@ -584,58 +614,102 @@ int enumerate_passes(Engine& e, const BatchOptions& opt, const GraphView& gv, co
   A.in_tasks = nullptr;
   A.in_count = 0;
   A.out_cap = kOverflowCap;
-  A.ctr = ctr;
+  A.ctr = R.ctr;
   A.chunk = std::max<uint32_t>(opt.chunk, 1);
+  A.budget = (long long)opt.budget_cycles;
   A.res = d_res;
   A.work_cap = opt.max_work;
   A.algo_bytes = d_misc + 1;
-  unsigned long long* d_ev = e.arena.take<unsigned long long>(8);
-  if (!d_ev) return fail(FSIG_EADMISSION, "arena");
-  FSIG_CUDA_TRY(cudaMemsetAsync(d_ev, 0, 64, s));
-  A.ev = d_ev;
+  A.ev = R.d_ev;
   A.seed = FSIG_HASH_SEED;
-  TaskRec* out = qa;
-  uint32_t* ready = ra;
-  TaskRec* other = qb;
-  uint32_t* other_ready = rb;
-  passes = 0;
-  FSIG_CUDA_TRY(cudaMemsetAsync(d_misc + 1, 0, sizeof(unsigned long long), s));
-  for (uint32_t pass = 0;; pass++) {
-    A.out_tasks = out;
-    A.out_ready = ready;
-    A.tag = pass + 1;
-    A.budget = (long long)opt.budget_cycles;
-    // every warp starts active; idle warps are counted as they wait
-    uint32_t init[8 * kCtrStride] = {0};
-    init[0] = pass == 0 ? opt.task_begin : 0u;
-    init[5 * kCtrStride] = uint32_t(e.num_sms * per_sm) * wpb;
-    FSIG_CUDA_TRY(cudaMemcpyAsync(ctr, init, sizeof(init), cudaMemcpyHostToDevice, s));
-    FSIG_CUDA_TRY(cudaEventRecord(e.ev_enum[0], s));
-    enumerate_kernel<<<e.num_sms * per_sm, wpb * 32, smem, s>>>(A);
-    FSIG_CUDA_TRY(cudaGetLastError());
-    FSIG_CUDA_TRY(cudaEventRecord(e.ev_enum[1], s));
-    passes++;
-    uint32_t hc[4 * kCtrStride];
-    FSIG_CUDA_TRY(cudaMemcpyAsync(hc, ctr, sizeof(hc), cudaMemcpyDeviceToHost, s));
-    FSIG_CUDA_TRY(cudaStreamSynchronize(s));
-    float ms = 0;
-    FSIG_CUDA_TRY(cudaEventElapsedTime(&ms, e.ev_enum[0], e.ev_enum[1]));
-    ms_enum += ms;
-    d2h += sizeof(hc);
-    const uint32_t h[4] = {hc[0], hc[kCtrStride], hc[2 * kCtrStride], hc[3 * kCtrStride]};
-    if (h[3] & kErrTimeout) return fail(FSIG_ETIMEOUT, "a work-queue record was not published in time");
-    const uint32_t head = h[2], tail = std::min(h[1], kOverflowCap);
-    if (head >= tail) break;
-    // unconsumed records become the next pass's input
-    A.in_tasks = out + head;
-    A.in_count = tail - head;
-    std::swap(out, other);
-    std::swap(ready, other_ready);
-    if (pass > 4096) return fail(FSIG_EOVERFLOW, "enumeration did not converge");
-  }
-  FSIG_CUDA_TRY(cudaMemcpyAsync(e.last_ev, d_ev, sizeof(e.last_ev), cudaMemcpyDeviceToHost, s));
-  FSIG_CUDA_TRY(cudaStreamSynchronize(s));
+  R.out = qa;
+  R.ready = ra;
+  R.other = qb;
+  R.other_ready = rb;
   return FSIG_OK;
+}
+
+int enum_launch(Engine& e, EnumRun& R) {
+  cudaStream_t s = e.stream;
+  R.A.out_tasks = R.out;
+  R.A.out_ready = R.ready;
+  R.A.tag = R.pass + 1;
+  ctr_init_kernel<<<1, 256, 0, s>>>(R.ctr, R.pass == 0 ? R.first_task : 0u, R.active);
+  FSIG_CUDA_TRY(cudaGetLastError());
+  FSIG_CUDA_TRY(cudaEventRecord(e.ev_enum[0], s));
+  enumerate_kernel<<<R.grid, R.block, R.smem, s>>>(R.A);
+  FSIG_CUDA_TRY(cudaGetLastError());
+  FSIG_CUDA_TRY(cudaEventRecord(e.ev_enum[1], s));
+  FSIG_CUDA_TRY(cudaMemcpyAsync(R.h_ctr, R.ctr, sizeof(uint32_t) * 4 * kCtrStride, cudaMemcpyDeviceToHost, s));
+  return FSIG_OK;
+}
+
+// Call once the stream has passed the pass's counter copy.  Sets more when
+// records are left for another pass, and readies that pass.
+int enum_after(Engine& e, EnumRun& R, bool& more, float& ms_enum, uint64_t& d2h) {
+  float ms = 0;
+  FSIG_CUDA_TRY(cudaEventElapsedTime(&ms, e.ev_enum[0], e.ev_enum[1]));
+  ms_enum += ms;
+  d2h += sizeof(uint32_t) * 4 * kCtrStride;
+  const uint32_t* hc = R.h_ctr;
+  if (hc[3 * kCtrStride] & kErrTimeout) return fail(FSIG_ETIMEOUT, "a work-queue record was not published in time");
+  const uint32_t head = hc[2 * kCtrStride], tail = std::min(hc[1 * kCtrStride], kOverflowCap);
+  more = head < tail;
+  if (!more) return FSIG_OK;
+  // unconsumed records become the next pass's input
+  R.A.in_tasks = R.out + head;
+  R.A.in_count = tail - head;
+  std::swap(R.out, R.other);
+  std::swap(R.ready, R.other_ready);
+  if (++R.pass > 4096) return fail(FSIG_EOVERFLOW, "enumeration did not converge");
+  return FSIG_OK;
+}
+
+// Page-locked host staging of one batch (inputs, then outputs), grown on
+// demand; graph-captured copies read and write it at replay.
+struct Stage {
+  uint8_t* base = nullptr;
+  size_t used = 0;
+  template <class T>
+  T* take(size_t n) {
+    used = (used + 255) & ~size_t(255);
+    T* p = reinterpret_cast<T*>(base + used);
+    used += sizeof(T) * n;
+    return p;
+  }
+};
+
+int reserve_pinned(Engine& e, size_t bytes) {
+  if (e.pinned_bytes >= bytes) return FSIG_OK;
+  if (e.pinned) cudaFreeHost(e.pinned);
+  e.pinned = nullptr;
+  e.pinned_bytes = 0;
+  const size_t want = std::max<size_t>(bytes + bytes / 4, size_t(1) << 20);
+  FSIG_CUDA_TRY(cudaHostAlloc(&e.pinned, want, cudaHostAllocDefault));
+  e.pinned_bytes = want;
+  return FSIG_OK;
+}
+
+template <class T>
+T* stage_upload(Engine& e, Stage& st, const std::vector<T>& v, int& rc) {
+  T* d = e.arena.take<T>(std::max<size_t>(v.size(), 1));
+  if (!d) { rc = fail(FSIG_EADMISSION, "batch does not fit the device arena"); return nullptr; }
+  T* h = st.take<T>(v.size());
+  if (!v.empty()) {
+    std::memcpy(h, v.data(), sizeof(T) * v.size());
+    cudaError_t err = cudaMemcpyAsync(d, h, sizeof(T) * v.size(), cudaMemcpyHostToDevice, e.stream);
+    if (err != cudaSuccess) { rc = fail_cuda(err, "cudaMemcpyAsync", __FILE__, __LINE__); return nullptr; }
+    e.cur_h2d += sizeof(T) * v.size();
+  }
+  return d;
+}
+
+size_t stage_bytes(const BatchLayout& b) {
+  const size_t a = 256;
+  const size_t Q = b.Q, G = b.G;
+  return 20 * a + sizeof(QVert) * G + 4 * (Q + 1) + 4 * b.lab_gidx.size() + 4 * b.lab_begin.size() +
+         8 * b.gword.size() + 4 * G + 4 * G + sizeof(QueryResult) * Q + 4 * G + 4 * Q * kMaxQ + sizeof(Plan) * Q +
+         8 + 4 * 4 * kCtrStride + 64;
 }
 }  // namespace
 
@@ -651,22 +725,26 @@ int run_batch(Engine& e, const std::vector<HostQuery>& qs, const BatchOptions& o
   out.orders.assign(size_t(Q) * kMaxQ, 0);
   out.ok.assign(Q, 0);
   if (Q == 0) return FSIG_OK;
-  if (b.root_cap > 0xffffffffull) return fail(FSIG_EADMISSION, "batch has more than 2^32 root candidates");
+  if (b.root_cap + 1 > 0xffffffffull) return fail(FSIG_EADMISSION, "batch has more than 2^32 root candidates");
+  if (opt.emit_cap && Q != 1) return fail(FSIG_EINVAL, "embedding output is for one query at a time");
+  // One CUDA graph per batch when every step is stream-ordered: orders chosen
+  // on the device and no embedding output.
+  const bool graph = opt.use_graph && !opt.host_order && !opt.emit_cap;
   e.arena.release(g.arena_mark);
   e.cur_h2d = 0;
   uint64_t d2h = 0;
   uint32_t launches = 0;
-  int rc = FSIG_OK;
-  QVert* d_qv = upload(e, b.qv, rc);
+  int rc = enum_configure(e);
   if (rc) return rc;
-  uint32_t* d_qoff = upload(e, b.qoff, rc);
+  if (opt.learned) {
+    rc = mpnn_configure(e);
+    if (rc) return rc;
+  }
+  rc = reserve_pinned(e, stage_bytes(b));
   if (rc) return rc;
-  uint32_t* d_lab_gidx = upload(e, b.lab_gidx, rc);
-  if (rc) return rc;
-  uint32_t* d_lab_begin = upload(e, b.lab_begin, rc);
-  if (rc) return rc;
-  uint64_t* d_gword = upload(e, b.gword, rc);
-  if (rc) return rc;
+  Stage st;
+  st.base = static_cast<uint8_t*>(e.pinned);
+
   std::vector<uint32_t> given(b.G, 0);
   std::vector<float> scores(b.G, 0.f);
   for (uint32_t q = 0; q < Q; q++)
@@ -674,143 +752,252 @@ int run_batch(Engine& e, const std::vector<HostQuery>& qs, const BatchOptions& o
       given[b.qoff[q] + i] = qs[q].has_given ? qs[q].given[i] : i;
       if (opt.scores) scores[b.qoff[q] + i] = opt.scores[b.qoff[q] + i];
     }
-  uint32_t* d_given = upload(e, given, rc);
-  if (rc) return rc;
-  float* d_scores = upload(e, scores, rc);
-  if (rc) return rc;
-  uint32_t* d_counts = e.arena.take<uint32_t>(std::max<uint32_t>(b.G, 1));
-  Plan* d_plans = e.arena.take<Plan>(Q);
-  uint32_t* d_rootcnt = e.arena.take<uint32_t>(uint64_t(Q) + 1);
-  uint32_t* d_rootoff = e.arena.take<uint32_t>(uint64_t(Q) + 1);
-  uint32_t* d_orders = e.arena.take<uint32_t>(uint64_t(Q) * kMaxQ);
-  QueryResult* d_res = e.arena.take<QueryResult>(Q);
-  unsigned long long* d_misc = e.arena.take<unsigned long long>(4);  // [1] modelled bytes
-  if (!d_counts || !d_plans || !d_rootcnt || !d_rootoff || !d_orders || !d_res || !d_misc)
-    return fail(FSIG_EADMISSION, "batch does not fit the device arena");
 
-  FSIG_CUDA_TRY(cudaEventRecord(e.ev[0], s));
-  uint32_t* pool = nullptr;
-  rc = filter_stage(e, b, opt.filter_mode, opt.refine_iters, d_qv, d_gword, d_lab_gidx, d_lab_begin, pool, d_counts,
-                    &launches);
-  if (rc) return rc;
-  FSIG_CUDA_TRY(cudaEventRecord(e.ev[1], s));
+  cudaGraph_t cg = nullptr;
+  if (graph) FSIG_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
+  EnumRun R;
+  QueryResult* h_res = nullptr;
+  uint32_t *h_counts = nullptr, *h_orders = nullptr, *d_chunk_off = nullptr, *d_rootoff = nullptr;
+  Plan* h_plans = nullptr;
+  unsigned long long* h_misc = nullptr;
+  unsigned long long* h_ev = nullptr;
+  QueryResult* d_res = nullptr;
+  unsigned long long* d_misc = nullptr;
+  Plan* d_plans = nullptr;
+  uint32_t *d_counts = nullptr, *d_orders = nullptr, *d_emit = nullptr;
+  unsigned long long* d_emit_ctr = nullptr;
 
-  uint32_t order_mode = opt.order_mode;
-  if (opt.host_order) {
-    // Reference-exact orders are computed on the host from the counts.
-    FSIG_CUDA_TRY(cudaMemcpyAsync(out.counts.data(), d_counts, sizeof(uint32_t) * b.G, cudaMemcpyDeviceToHost, s));
-    FSIG_CUDA_TRY(cudaStreamSynchronize(s));
-    d2h += sizeof(uint32_t) * b.G;
-    for (uint32_t q = 0; q < Q; q++) {
-      bool any_zero = false;
-      for (uint32_t u = 0; u < qs[q].n; u++) any_zero |= out.counts[b.qoff[q] + u] == 0;
-      if (qs[q].has_given) continue;
-      if (any_zero) {  // nothing to enumerate; any connected order will do
-        for (uint32_t i = 0; i < qs[q].n; i++) given[b.qoff[q] + i] = i;
-        uint32_t placed = 1u;
-        for (uint32_t i = 1; i < qs[q].n; i++)
-          for (uint32_t u = 0; u < qs[q].n; u++)
-            if (!((placed >> u) & 1u) && (qs[q].adj[u] & placed)) { given[b.qoff[q] + i] = u; placed |= 1u << u; break; }
-        continue;
+  // Everything from the uploads to the results' copy back, in stream order.
+  auto enqueue = [&]() -> int {
+    int rc = FSIG_OK;
+    FSIG_CUDA_TRY(cudaEventRecord(e.ev[0], s));
+    QVert* d_qv = stage_upload(e, st, b.qv, rc);
+    if (rc) return rc;
+    uint32_t* d_qoff = stage_upload(e, st, b.qoff, rc);
+    if (rc) return rc;
+    uint32_t* d_lab_gidx = stage_upload(e, st, b.lab_gidx, rc);
+    if (rc) return rc;
+    uint32_t* d_lab_begin = stage_upload(e, st, b.lab_begin, rc);
+    if (rc) return rc;
+    uint64_t* d_gword = stage_upload(e, st, b.gword, rc);
+    if (rc) return rc;
+    uint32_t* d_given = stage_upload(e, st, given, rc);
+    if (rc) return rc;
+    float* d_scores = stage_upload(e, st, scores, rc);
+    if (rc) return rc;
+    d_counts = e.arena.take<uint32_t>(std::max<uint32_t>(b.G, 1));
+    d_plans = e.arena.take<Plan>(Q);
+    uint32_t* d_rootcnt = e.arena.take<uint32_t>(uint64_t(Q) + 1);
+    d_rootoff = e.arena.take<uint32_t>(uint64_t(Q) + 1);
+    d_orders = e.arena.take<uint32_t>(uint64_t(Q) * kMaxQ);
+    d_res = e.arena.take<QueryResult>(Q);
+    d_misc = e.arena.take<unsigned long long>(4);  // [1] modelled bytes
+    if (!d_counts || !d_plans || !d_rootcnt || !d_rootoff || !d_orders || !d_res || !d_misc)
+      return fail(FSIG_EADMISSION, "batch does not fit the device arena");
+    h_res = st.take<QueryResult>(Q);
+    h_counts = st.take<uint32_t>(b.G);
+    h_orders = st.take<uint32_t>(size_t(Q) * kMaxQ);
+    h_plans = st.take<Plan>(Q);
+    h_misc = st.take<unsigned long long>(1);
+    uint32_t* h_ctr = st.take<uint32_t>(4 * kCtrStride);
+    h_ev = st.take<unsigned long long>(8);
+
+    uint32_t* pool = nullptr;
+    rc = filter_stage(e, b, opt.filter_mode, opt.refine_iters, d_qv, d_gword, d_lab_gidx, d_lab_begin, pool,
+                      d_counts, &launches);
+    if (rc) return rc;
+    FSIG_CUDA_TRY(cudaEventRecord(e.ev[1], s));
+
+    uint32_t order_mode = opt.order_mode;
+    if (opt.host_order) {
+      // Reference-exact orders are computed on the host from the counts.
+      FSIG_CUDA_TRY(cudaMemcpyAsync(out.counts.data(), d_counts, sizeof(uint32_t) * b.G, cudaMemcpyDeviceToHost, s));
+      FSIG_CUDA_TRY(cudaStreamSynchronize(s));
+      d2h += sizeof(uint32_t) * b.G;
+      for (uint32_t q = 0; q < Q; q++) {
+        bool any_zero = false;
+        for (uint32_t u = 0; u < qs[q].n; u++) any_zero |= out.counts[b.qoff[q] + u] == 0;
+        if (qs[q].has_given) continue;
+        if (any_zero) {  // nothing to enumerate; any connected order will do
+          for (uint32_t i = 0; i < qs[q].n; i++) given[b.qoff[q] + i] = i;
+          uint32_t placed = 1u;
+          for (uint32_t i = 1; i < qs[q].n; i++)
+            for (uint32_t u = 0; u < qs[q].n; u++)
+              if (!((placed >> u) & 1u) && (qs[q].adj[u] & placed)) { given[b.qoff[q] + i] = u; placed |= 1u << u; break; }
+          continue;
+        }
+        opt.host_order(qs[q], out.counts.data() + b.qoff[q], given.data() + b.qoff[q]);
       }
-      opt.host_order(qs[q], out.counts.data() + b.qoff[q], given.data() + b.qoff[q]);
+      FSIG_CUDA_TRY(cudaMemcpyAsync(d_given, given.data(), sizeof(uint32_t) * b.G, cudaMemcpyHostToDevice, s));
+      e.cur_h2d += sizeof(uint32_t) * b.G;
+      order_mode = kOrderGiven;
     }
-    FSIG_CUDA_TRY(cudaMemcpyAsync(d_given, given.data(), sizeof(uint32_t) * b.G, cudaMemcpyHostToDevice, s));
-    e.cur_h2d += sizeof(uint32_t) * b.G;
-    order_mode = kOrderGiven;
-  }
-  const float* d_score_src = d_scores;
-  if (opt.learned) {
-    // Order-network scores from the filtered candidate counts, on the device;
-    // the algorithm's own heuristic order is one of the inputs.
-    float* d_feat = e.arena.take<float>(uint64_t(std::max<uint32_t>(b.G, 1)) * kFeat);
-    uint32_t* d_nbr = e.arena.take<uint32_t>(std::max<uint32_t>(b.G, 1));
-    float* d_lscores = e.arena.take<float>(std::max<uint32_t>(b.G, 1));
-    if (!d_feat || !d_nbr || !d_lscores) return fail(FSIG_EADMISSION, "order-network inputs do not fit the arena");
-    order_kernel<<<(Q + 7) / 8, 256, 0, s>>>(d_qv, d_qoff, Q, d_counts, order_mode, d_scores, d_given, d_plans,
+    const float* d_score_src = d_scores;
+    if (opt.learned) {
+      // Order-network scores from the filtered candidate counts, on the
+      // device; the algorithm's own heuristic order is one of the inputs.
+      float* d_feat = e.arena.take<float>(uint64_t(std::max<uint32_t>(b.G, 1)) * kFeat);
+      uint32_t* d_nbr = e.arena.take<uint32_t>(std::max<uint32_t>(b.G, 1));
+      float* d_lscores = e.arena.take<float>(std::max<uint32_t>(b.G, 1));
+      if (!d_feat || !d_nbr || !d_lscores) return fail(FSIG_EADMISSION, "order-network inputs do not fit the arena");
+      order_kernel<<<(Q + 7) / 8, 256, 0, s>>>(d_qv, d_qoff, Q, d_counts, order_mode, d_scores, d_given, d_plans,
+                                               d_rootcnt, d_orders);
+      FSIG_CUDA_TRY(cudaGetLastError());
+      rc = mpnn_features_device(e, d_qv, b.G, d_qoff, Q, d_counts, d_orders, d_feat, d_nbr);
+      if (rc) return rc;
+      rc = mpnn_forward_device(e, Q, d_qoff, d_feat, d_nbr, d_lscores);
+      if (rc) return rc;
+      launches += 3;
+      d_score_src = d_lscores;
+      order_mode = kOrderScores;
+    }
+    uint32_t* d_roots = e.arena.take<uint32_t>(std::max<uint64_t>(b.root_cap, 1));
+    uint32_t* d_root_q = e.arena.take<uint32_t>(std::max<uint64_t>(b.root_cap, 1));
+    uint32_t* d_chunks = e.arena.take<uint32_t>(b.root_cap + 1);
+    d_chunk_off = e.arena.take<uint32_t>(b.root_cap + 1);
+    if (!d_roots || !d_root_q || !d_chunks || !d_chunk_off)
+      return fail(FSIG_EADMISSION, "root list does not fit the device arena");
+    FSIG_CUDA_TRY(cudaMemsetAsync(d_rootcnt, 0, sizeof(uint32_t) * (uint64_t(Q) + 1), s));
+    order_kernel<<<(Q + 7) / 8, 256, 0, s>>>(d_qv, d_qoff, Q, d_counts, order_mode, d_score_src, d_given, d_plans,
                                              d_rootcnt, d_orders);
     FSIG_CUDA_TRY(cudaGetLastError());
-    rc = mpnn_features_device(e, d_qv, b.G, d_qoff, Q, d_counts, d_orders, d_feat, d_nbr);
+    rc = device_exclusive_scan<uint32_t>(e.arena, d_rootcnt, d_rootoff, uint64_t(Q) + 1, nullptr, s, &launches);
     if (rc) return rc;
-    rc = mpnn_forward_device(e, Q, d_qoff, d_feat, d_nbr, d_lscores);
-    if (rc) return rc;
-    launches += 3;
-    d_score_src = d_lscores;
-    order_mode = kOrderScores;
-  }
-  uint32_t* d_roots = e.arena.take<uint32_t>(std::max<uint64_t>(b.root_cap, 1));
-  uint32_t* d_root_q = e.arena.take<uint32_t>(std::max<uint64_t>(b.root_cap, 1));
-  uint32_t* d_chunks = e.arena.take<uint32_t>(std::max<uint64_t>(b.root_cap, 1) + 1);
-  uint32_t* d_chunk_off = e.arena.take<uint32_t>(std::max<uint64_t>(b.root_cap, 1) + 1);
-  if (!d_roots || !d_root_q || !d_chunks || !d_chunk_off)
-    return fail(FSIG_EADMISSION, "root list does not fit the device arena");
-  FSIG_CUDA_TRY(cudaMemsetAsync(d_rootcnt, 0, sizeof(uint32_t) * (uint64_t(Q) + 1), s));
-  order_kernel<<<(Q + 7) / 8, 256, 0, s>>>(d_qv, d_qoff, Q, d_counts, order_mode, d_score_src, d_given, d_plans,
-                                           d_rootcnt, d_orders);
-  FSIG_CUDA_TRY(cudaGetLastError());
-  rc = device_exclusive_scan<uint32_t>(e.arena, d_rootcnt, d_rootoff, uint64_t(Q) + 1, nullptr, s, &launches);
-  if (rc) return rc;
-  roots_kernel<<<std::min<uint32_t>(Q, e.num_sms * 8), 256, 0, s>>>(d_qv, d_plans, Q, d_rootoff, pool, d_roots,
-                                                                     d_root_q);
-  FSIG_CUDA_TRY(cudaGetLastError());
-  launches += 2;
-  // pass-0 task space: depth-1 chunks of every root
-  uint32_t nroots = 0;
-  FSIG_CUDA_TRY(cudaMemcpyAsync(&nroots, d_rootoff + Q, 4, cudaMemcpyDeviceToHost, s));
-  FSIG_CUDA_TRY(cudaStreamSynchronize(s));
-  d2h += 4;
-  const uint32_t split = std::max<uint32_t>(opt.split, 32);
-  FSIG_CUDA_TRY(cudaMemsetAsync(d_chunks, 0, sizeof(uint32_t) * (uint64_t(nroots) + 1), s));
-  if (nroots) {
-    root_chunks_kernel<<<grid_cap(nroots, 256, e.num_sms, 8), 256, 0, s>>>(view_of(g), d_plans, d_roots, d_root_q,
-                                                                          d_rootoff + Q, split, d_chunks);
+    roots_kernel<<<std::min<uint32_t>(Q, e.num_sms * 8), 256, 0, s>>>(d_qv, d_plans, Q, d_rootoff, pool, d_roots,
+                                                                       d_root_q);
     FSIG_CUDA_TRY(cudaGetLastError());
-    launches++;
-  }
-  rc = device_exclusive_scan<uint32_t>(e.arena, d_chunks, d_chunk_off, uint64_t(nroots) + 1, nullptr, s, &launches);
-  if (rc) return rc;
-  FSIG_CUDA_TRY(cudaMemsetAsync(d_res, 0, sizeof(QueryResult) * Q, s));
-  uint32_t* d_emit = nullptr;
-  unsigned long long* d_emit_ctr = nullptr;
-  if (opt.emit_cap) {
-    if (Q != 1) return fail(FSIG_EINVAL, "embedding output is for one query at a time");
-    d_emit_ctr = e.arena.take<unsigned long long>(1);
-    d_emit = e.arena.take<uint32_t>(opt.emit_cap * qs[0].n);
-    if (!d_emit || !d_emit_ctr) return fail(FSIG_EADMISSION, "embedding buffer does not fit the device arena");
-    FSIG_CUDA_TRY(cudaMemsetAsync(d_emit_ctr, 0, sizeof(unsigned long long), s));
-  }
-  rc = enumerate_passes(e, opt, view_of(g), d_plans, pool, Q, d_roots, d_root_q, d_chunk_off, nroots, split, d_res,
-                        d_misc, d_emit, d_emit_ctr, out.passes, out.ms_enum, d2h);
-  if (rc) return rc;
-  if (opt.emit_cap) {
-    FSIG_CUDA_TRY(cudaMemcpyAsync(&out.emit_total, d_emit_ctr, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
-    FSIG_CUDA_TRY(cudaMemcpyAsync(&out.tasks_total, d_chunk_off + nroots, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-    FSIG_CUDA_TRY(cudaStreamSynchronize(s));
-    const uint64_t rows = std::min<uint64_t>(out.emit_total, opt.emit_cap);
-    out.rows.resize(rows * qs[0].n);
-    if (rows)
-      FSIG_CUDA_TRY(cudaMemcpyAsync(out.rows.data(), d_emit, sizeof(uint32_t) * rows * qs[0].n,
-                                    cudaMemcpyDeviceToHost, s));
-    d2h += 12 + sizeof(uint32_t) * rows * qs[0].n;
-  }
-  launches += out.passes;
-  FSIG_CUDA_TRY(cudaEventRecord(e.ev[2], s));
+    launches += 2;
+    // Pass-0 task space: depth-1 chunks of every root.  Sized by the bound
+    // on the number of roots (the count itself stays on the device).
+    // (embedding output may cut the depth-1 ranges as finely as one entry)
+    const uint32_t split = std::max<uint32_t>(opt.split, opt.emit_cap ? 1u : 32u);
+    FSIG_CUDA_TRY(cudaMemsetAsync(d_chunks, 0, sizeof(uint32_t) * (b.root_cap + 1), s));
+    if (b.root_cap) {
+      root_chunks_kernel<<<grid_cap(b.root_cap, 256, e.num_sms, 8), 256, 0, s>>>(view_of(g), d_plans, d_roots,
+                                                                                  d_root_q, d_rootoff + Q, split,
+                                                                                  d_chunks);
+      FSIG_CUDA_TRY(cudaGetLastError());
+      launches++;
+    }
+    rc = device_exclusive_scan<uint32_t>(e.arena, d_chunks, d_chunk_off, b.root_cap + 1, nullptr, s, &launches);
+    if (rc) return rc;
+    FSIG_CUDA_TRY(cudaMemsetAsync(d_res, 0, sizeof(QueryResult) * Q, s));
+    if (opt.emit_cap) {
+      d_emit_ctr = e.arena.take<unsigned long long>(1);
+      d_emit = e.arena.take<uint32_t>(opt.emit_cap * qs[0].n);
+      if (!d_emit || !d_emit_ctr) return fail(FSIG_EADMISSION, "embedding buffer does not fit the device arena");
+      FSIG_CUDA_TRY(cudaMemsetAsync(d_emit_ctr, 0, sizeof(unsigned long long), s));
+    }
+    rc = enum_prepare(e, opt, view_of(g), d_plans, pool, Q, d_roots, d_root_q, d_chunk_off, d_rootoff + Q, split,
+                      d_res, d_misc, d_emit, d_emit_ctr, h_ctr, R);
+    if (rc) return rc;
+    return enum_launch(e, R);
+  };
+  // The results' copy back (after the last pass).
+  auto copy_back = [&]() -> int {
+    FSIG_CUDA_TRY(cudaEventRecord(e.ev[2], s));
+    FSIG_CUDA_TRY(cudaMemcpyAsync(h_res, d_res, sizeof(QueryResult) * Q, cudaMemcpyDeviceToHost, s));
+    FSIG_CUDA_TRY(cudaMemcpyAsync(h_counts, d_counts, sizeof(uint32_t) * b.G, cudaMemcpyDeviceToHost, s));
+    FSIG_CUDA_TRY(cudaMemcpyAsync(h_orders, d_orders, sizeof(uint32_t) * Q * kMaxQ, cudaMemcpyDeviceToHost, s));
+    FSIG_CUDA_TRY(cudaMemcpyAsync(h_misc, d_misc + 1, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    FSIG_CUDA_TRY(cudaMemcpyAsync(h_plans, d_plans, sizeof(Plan) * Q, cudaMemcpyDeviceToHost, s));
+    FSIG_CUDA_TRY(cudaMemcpyAsync(h_ev, R.d_ev, sizeof(e.last_ev), cudaMemcpyDeviceToHost, s));
+    return FSIG_OK;
+  };
 
-  FSIG_CUDA_TRY(cudaMemcpyAsync(out.res.data(), d_res, sizeof(QueryResult) * Q, cudaMemcpyDeviceToHost, s));
-  FSIG_CUDA_TRY(cudaMemcpyAsync(out.counts.data(), d_counts, sizeof(uint32_t) * b.G, cudaMemcpyDeviceToHost, s));
-  FSIG_CUDA_TRY(cudaMemcpyAsync(out.orders.data(), d_orders, sizeof(uint32_t) * Q * kMaxQ, cudaMemcpyDeviceToHost, s));
-  FSIG_CUDA_TRY(cudaMemcpyAsync(&out.algo_bytes, d_misc + 1, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
-  std::vector<Plan> hp(Q);
-  FSIG_CUDA_TRY(cudaMemcpyAsync(hp.data(), d_plans, sizeof(Plan) * Q, cudaMemcpyDeviceToHost, s));
-  FSIG_CUDA_TRY(cudaStreamSynchronize(s));
-  for (uint32_t q = 0; q < Q; q++) out.ok[q] = hp[q].ok;
+  bool more = false;
+  out.passes = 0;
+  out.ms_enum = 0;
+  if (graph) {
+    rc = enqueue();
+    if (!rc) rc = copy_back();
+    const cudaError_t end = cudaStreamEndCapture(s, &cg);
+    if (rc) {
+      if (cg) cudaGraphDestroy(cg);
+      return rc;
+    }
+    if (end != cudaSuccess) return fail_cuda(end, "cudaStreamEndCapture", __FILE__, __LINE__);
+    if (e.gexec) {
+      cudaGraphExecUpdateResultInfo info;
+      if (cudaGraphExecUpdate(e.gexec, cg, &info) != cudaSuccess) {
+        cudaGetLastError();
+        cudaGraphExecDestroy(e.gexec);
+        e.gexec = nullptr;
+      }
+    }
+    if (!e.gexec) {
+      const cudaError_t err = cudaGraphInstantiate(&e.gexec, cg, 0);
+      if (err != cudaSuccess) {
+        cudaGraphDestroy(cg);
+        e.gexec = nullptr;
+        return fail_cuda(err, "cudaGraphInstantiate", __FILE__, __LINE__);
+      }
+    }
+    cudaGraphDestroy(cg);
+    FSIG_CUDA_TRY(cudaGraphLaunch(e.gexec, s));
+    FSIG_CUDA_TRY(cudaStreamSynchronize(s));
+    out.passes = 1;
+    rc = enum_after(e, R, more, out.ms_enum, d2h);
+    if (rc) return rc;
+    if (more) {  // records left over: further passes run as ordinary launches
+      while (more) {
+        rc = enum_launch(e, R);
+        if (rc) return rc;
+        FSIG_CUDA_TRY(cudaStreamSynchronize(s));
+        out.passes++;
+        rc = enum_after(e, R, more, out.ms_enum, d2h);
+        if (rc) return rc;
+      }
+      rc = copy_back();
+      if (rc) return rc;
+      FSIG_CUDA_TRY(cudaStreamSynchronize(s));
+    }
+  } else {
+    rc = enqueue();
+    if (rc) return rc;
+    do {
+      FSIG_CUDA_TRY(cudaStreamSynchronize(s));
+      out.passes++;
+      rc = enum_after(e, R, more, out.ms_enum, d2h);
+      if (rc) return rc;
+      if (more) {
+        rc = enum_launch(e, R);
+        if (rc) return rc;
+      }
+    } while (more);
+    if (opt.emit_cap) {
+      uint32_t nroots = 0;
+      FSIG_CUDA_TRY(cudaMemcpyAsync(&nroots, d_rootoff + Q, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+      FSIG_CUDA_TRY(cudaMemcpyAsync(&out.emit_total, d_emit_ctr, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+      FSIG_CUDA_TRY(cudaStreamSynchronize(s));
+      FSIG_CUDA_TRY(cudaMemcpyAsync(&out.tasks_total, d_chunk_off + nroots, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+      FSIG_CUDA_TRY(cudaStreamSynchronize(s));
+      const uint64_t rows = std::min<uint64_t>(out.emit_total, opt.emit_cap);
+      out.rows.resize(rows * qs[0].n);
+      if (rows)
+        FSIG_CUDA_TRY(cudaMemcpyAsync(out.rows.data(), d_emit, sizeof(uint32_t) * rows * qs[0].n,
+                                      cudaMemcpyDeviceToHost, s));
+      d2h += 16 + sizeof(uint32_t) * rows * qs[0].n;
+    }
+    rc = copy_back();
+    if (rc) return rc;
+    FSIG_CUDA_TRY(cudaStreamSynchronize(s));
+  }
+  launches += out.passes * 2;  // counter reset + enumeration per pass
+  std::memcpy(out.res.data(), h_res, sizeof(QueryResult) * Q);
+  std::memcpy(out.counts.data(), h_counts, sizeof(uint32_t) * b.G);
+  std::memcpy(out.orders.data(), h_orders, sizeof(uint32_t) * Q * kMaxQ);
+  std::memcpy(e.last_ev, h_ev, sizeof(e.last_ev));
+  out.algo_bytes = *h_misc;
+  for (uint32_t q = 0; q < Q; q++) out.ok[q] = h_plans[q].ok;
   FSIG_CUDA_TRY(cudaEventElapsedTime(&out.ms_filter, e.ev[0], e.ev[1]));
   FSIG_CUDA_TRY(cudaEventElapsedTime(&out.ms_join, e.ev[1], e.ev[2]));
   d2h += sizeof(QueryResult) * Q + sizeof(uint32_t) * b.G + sizeof(uint32_t) * Q * kMaxQ +
-         sizeof(unsigned long long) + sizeof(Plan) * Q;
+         sizeof(unsigned long long) + sizeof(Plan) * Q + sizeof(e.last_ev);
   out.h2d_bytes = e.cur_h2d;
   out.d2h_bytes = d2h;
   out.launches = launches;
+  out.graph = graph;
   e.last.h2d_bytes = out.h2d_bytes;
   e.last.d2h_bytes = out.d2h_bytes;
   e.last.enum_bytes = out.algo_bytes;
@@ -824,6 +1011,7 @@ int run_batch(Engine& e, const std::vector<HostQuery>& qs, const BatchOptions& o
   e.last.enum_handoffs = e.last_ev[2];
   e.last.enum_records = e.last_ev[3];
   e.last.enum_examines = e.last_ev[4];
+  e.last.graph = graph ? 1u : 0u;
   e.arena.release(g.arena_mark);
   return FSIG_OK;
 }
@@ -844,11 +1032,12 @@ int run_embeddings(Engine& e, const HostQuery& q, BatchOptions opt, uint64_t buf
   }
   // More embeddings than one buffer holds: cut the task space into ranges,
   // matched one after the other, halving a range whose rows still overflow.
-  // Tasks are made as small as they go (32 depth-1 entries) so that a range
-  // of one task is unlikely to overflow; an empty range gives their number.
+  // Tasks are made as small as they go (one depth-1 entry under one root) so
+  // that a range of one task is unlikely to overflow; an empty range gives
+  // their number.
   first.rows.clear();
   const uint64_t total = first.res[0].count;
-  opt.split = 32;
+  opt.split = 1;
   opt.task_begin = 0;
   opt.task_end = 0;
   BatchOutput probe;

@@ -91,6 +91,9 @@ struct BatchOptions {
   // BatchOutput::rows, and enumerate only pass-0 tasks [task_begin, task_end).
   uint64_t emit_cap = 0;
   uint32_t task_begin = 0, task_end = 0xffffffffu;
+  // Run the batch as one CUDA graph (uploads, filter, order, roots, first
+  // enumeration pass, results back) when orders are chosen on the device.
+  bool use_graph = false;
   // When set, candidate counts are brought to the host after filtering and
   // this function chooses each query's order (the reference-exact orders).
   void (*host_order)(const HostQuery&, const uint32_t* cand, uint32_t* order) = nullptr;
@@ -110,6 +113,7 @@ struct BatchOutput {
   std::vector<uint32_t> rows;   // emitted embeddings, n per row (emit_cap > 0)
   uint64_t emit_total = 0;      // embeddings found in the task range
   uint32_t tasks_total = 0;     // size of the pass-0 task space (emit_cap > 0)
+  bool graph = false;           // ran as a CUDA graph
 };
 
 // Runs filter -> refine -> order -> roots -> enumerate for a batch.

@@ -364,12 +364,12 @@ int launch_graph_kernel(Engine& e, bool train, uint32_t num_graphs, const uint32
   const size_t smem = graph_kernel_smem();
   const unsigned grid = std::max(1u, std::min<unsigned>((num_graphs + kWarpsPerBlock - 1) / kWarpsPerBlock,
                                                        unsigned(e.num_sms) * 4));
+  int rc = mpnn_configure(e);
+  if (rc) return rc;
   if (train) {
-    FSIG_CUDA_TRY(cudaFuncSetAttribute(mpnn_graph_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     mpnn_graph_kernel<true><<<grid, 32 * kWarpsPerBlock, smem, e.stream>>>(
         M.wbf, M.master, num_graphs, d_goff, d_feat, d_nbr, d_scores, d_target, inv_count, M.grad, d_loss, d_acts);
   } else {
-    FSIG_CUDA_TRY(cudaFuncSetAttribute(mpnn_graph_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     mpnn_graph_kernel<false><<<grid, 32 * kWarpsPerBlock, smem, e.stream>>>(
         M.wbf, M.master, num_graphs, d_goff, d_feat, d_nbr, d_scores, nullptr, 0.f, nullptr, nullptr, nullptr);
   }
@@ -378,6 +378,15 @@ int launch_graph_kernel(Engine& e, bool train, uint32_t num_graphs, const uint32
 }
 
 }  // namespace
+
+int mpnn_configure(Engine& e) {
+  if (e.mpnn_configured) return FSIG_OK;
+  const int smem = int(graph_kernel_smem());
+  FSIG_CUDA_TRY(cudaFuncSetAttribute(mpnn_graph_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  FSIG_CUDA_TRY(cudaFuncSetAttribute(mpnn_graph_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  e.mpnn_configured = true;
+  return FSIG_OK;
+}
 
 int mpnn_init(Engine& e) {
   if (e.mpnn) return FSIG_OK;

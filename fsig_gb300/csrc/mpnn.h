@@ -46,6 +46,9 @@ __host__ __device__ inline float plog2(uint32_t x) {
 
 struct QVert;
 int mpnn_init(Engine& e);
+// Shared-memory attributes of the network kernels (once per engine, before
+// any stream capture).
+int mpnn_configure(Engine& e);
 void mpnn_free(Engine& e);
 // Features of the batch's query vertices from their candidate counts and the
 // heuristic order (d_orders: Q x 32 vertex ids by position), on the device;

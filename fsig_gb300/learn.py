@@ -266,7 +266,7 @@ def match_learned(engine: Engine, queries: Sequence[Query], algo: int = ALGO_FUS
 # training the packaged network: logs on the mid-scale graphs
 # ---------------------------------------------------------------------------
 def training_workloads():
-    """(name, graph builder, query specs) of the logs the packaged network is
+    """(name, graph builder, query specs, work limit) of the logs the packaged network is
     trained on: the 320k-vertex Chung-Lu graph (exponent 2.1, seed 2, 16 Zipf
     labels) with 8-vertex and 4-32-vertex dense and sparse random-walk queries,
     and the unlabeled 2^20-vertex R-MAT graph (seed 3, 2^24 edges) with
@@ -285,8 +285,8 @@ def training_workloads():
     mixed = [(int(n), QUERY_DENSE if i % 2 else QUERY_SPARSE, 70_000_000 + i, 4)
              for i, n in enumerate(rng.integers(4, 33, 3000))]
     eight = [(8, QUERY_DENSE if i % 2 else QUERY_SPARSE, 71_000_000 + i, 4) for i in range(600)]
-    five = [(5, QUERY_INDUCED, 72_000_000 + i) for i in range(300)]
-    return [("chung-lu 320k", chung_lu, mixed + eight), ("r-mat 2^20 unlabeled", rmat, five)]
+    five = [(5, QUERY_INDUCED, 72_000_000 + i) for i in range(96)]
+    return [("chung-lu 320k", chung_lu, mixed + eight, 1 << 26), ("r-mat 2^20 unlabeled", rmat, five, 1 << 28)]
 
 
 def main(argv=None):
@@ -299,18 +299,19 @@ def main(argv=None):
     ap.add_argument("--per-query", type=int, default=16)
     ap.add_argument("--epochs", type=int, default=60)
     ap.add_argument("--lr", type=float, default=2e-3)
-    ap.add_argument("--work-limit", type=int, default=1 << 24, help="drop queries whose heuristic run examines more")
+    ap.add_argument("--work-limit", type=int, default=0,
+                    help="drop queries whose heuristic run examines more (default: per workload)")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--device", type=int, default=0)
     args = ap.parse_args(argv)
     logs = []
     with Engine(args.device, arena_bytes=48 << 30) as e:
         t0 = time.time()
-        for name, build, specs in training_workloads():
+        for name, build, specs, limit in training_workloads():
             g = build()
             csr = g.csr()
             e.load_graph(g)
-            qs = select_within_budget(e, gen_queries(g, specs, csr=csr), len(specs), args.work_limit)
+            qs = select_within_budget(e, gen_queries(g, specs, csr=csr), len(specs), args.work_limit or limit)
             lg = collect_logs(e, qs, per_query=args.per_query, seed=args.seed)
             gain = sum(x.heuristic_work for x in lg) / max(sum(x.best[1] for x in lg), 1)
             print(f"[learn] {name}: {len(lg)} queries logged, best/heuristic total work 1/{gain:.3f}, "

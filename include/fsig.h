@@ -189,7 +189,7 @@ typedef struct {
   float ms_filter;           /* device time, filter + refinement + counts       */
   float ms_join;             /* device time, ordering + roots + enumeration     */
   float ms_enum;             /* device time of the enumeration kernel launches  */
-  float pad;
+  uint32_t graph;            /* 1 when the batch ran as one CUDA graph          */
   uint64_t enum_tasks;       /* tasks run by the enumeration kernel             */
   uint64_t enum_pops;        /* handed-off records taken within the same pass   */
   uint64_t enum_handoffs;    /* frontier hand-offs                              */

@@ -289,3 +289,20 @@ def test_work_splitting_preserves_results(engine, config2_small):
         assert [(x.count, x.hash, x.level_counts) for x in r] == [(x.count, x.hash, x.level_counts) for x in base]
     single = [engine.match_batch([q], algo=F.ALGO_FUSED, split_cycles=2000, split_len=32)[0] for q in qs[:6]]
     assert [(x.count, x.hash) for x in single] == [(x.count, x.hash) for x in base[:6]]
+
+
+@pytest.mark.parametrize("algo", [F.ALGO_FSIG, F.ALGO_GSI, F.ALGO_FUSED])
+def test_cuda_graph_batches_match_stream_batches(engine, config2_small, algo):
+    """A batch run as one CUDA graph (replayed with updated parameters batch
+    after batch) returns what the same batch returns as ordinary launches,
+    including when records overflow into further passes after the graph."""
+    g, off, adj, qs = config2_small
+    engine.load_graph(g)
+    base = engine.match_batch(qs, algo=algo)
+    assert engine.last_stats()["graph"] == 0
+    want = [(x.count, x.hash, x.level_counts, x.order) for x in base]
+    for kw in (dict(), dict(split_cycles=2000, split_len=32, chunk=1)):
+        for part in (qs, qs[: len(qs) // 2], qs):  # different shapes, then the first again
+            r = engine.match_batch(part, algo=algo, use_graph=True, **kw)
+            assert engine.last_stats()["graph"] == 1
+            assert [(x.count, x.hash, x.level_counts, x.order) for x in r] == want[: len(part)]
