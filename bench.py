@@ -281,14 +281,14 @@ class StepStats:
         self.d2h += st["d2h_bytes"]
 
 
-def learned_step(e, b, algo, limit, acc):
+def learned_step(e, b, algo, limit, acc, use_graph):
     """One batch in learned order; queries over the work limit run again in
     heuristic order (the fallback).  Returns (results, fallbacks)."""
-    rs = e.match_batch(b, algo=algo, order_source=F.ORDER_LEARNED, max_work=limit)
+    rs = e.match_batch(b, algo=algo, order_source=F.ORDER_LEARNED, max_work=limit, use_graph=use_graph)
     acc.add(e.last_stats())
     redo = [i for i, r in enumerate(rs) if r.status == F.ELIMIT]
     if redo:
-        again = e.match_batch([b[i] for i in redo], algo=algo, order_source=F.ORDER_HEURISTIC)
+        again = e.match_batch([b[i] for i in redo], algo=algo, order_source=F.ORDER_HEURISTIC, use_graph=use_graph)
         acc.add(e.last_stats())
         for i, r in zip(redo, again):
             rs[i] = r
@@ -308,10 +308,12 @@ def run_ours(args, dist):
             e.mpnn_set_params(learn.load_params())
         limit = args.max_work or (WORK_BUDGET if order == "learned" else 0)
 
+        use_graph = not args.no_graph
+
         def step(b, acc):
             if order == "learned":
-                return learned_step(e, b, algo, limit, acc)
-            rs = e.match_batch(b, algo=algo, order_source=F.ORDER_HEURISTIC, max_work=limit)
+                return learned_step(e, b, algo, limit, acc, use_graph)
+            rs = e.match_batch(b, algo=algo, order_source=F.ORDER_HEURISTIC, max_work=limit, use_graph=use_graph)
             acc.add(e.last_stats())
             return rs, 0
 
@@ -347,7 +349,7 @@ def run_ours(args, dist):
         identical = True
         for k in range(args.steps):
             b = batches[k % len(batches)]
-            rs = e.match_batch(b, algo=algo, order_source=F.ORDER_HEURISTIC)
+            rs = e.match_batch(b, algo=algo, order_source=F.ORDER_HEURISTIC, use_graph=use_graph)
             heur.add(e.last_stats())
             identical &= [(r.count, r.hash) for r in rs] == results[k]
         dev_ms, enum_ms, enum_bytes = acc.dev_ms, acc.enum_ms, acc.enum_bytes
@@ -386,7 +388,7 @@ def run_ours(args, dist):
                    "algo": args.algo, "order": order, "parallelism": f"replicas x{dist.world}, queries sharded",
                    "l2": "inputs larger than L2 (resident graph arrays > 129 MB)" if args.workload in ("c5",) else
                    "graph fits L2; batches differ step to step",
-                   "work_limit": limit, "queries_over_limit": over, "learned_fallbacks": fallbacks,
+                   "work_limit": limit, "cuda_graph": use_graph, "queries_over_limit": over, "learned_fallbacks": fallbacks,
                    "selection": f"first queries of a seeded random-walk sequence whose enumeration examines at most "
                                 f"{WORK_BUDGET} driver entries"},
         "e2e": {"value": round(tot_q / wall_s, 3), "unit": "queries/s",
@@ -473,6 +475,7 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--ref-step-s", type=float, default=8.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-graph", action="store_true", help="ordinary launches instead of one CUDA graph per batch")
     ap.add_argument("--single-sample", type=int, default=64)
     args = ap.parse_args()
     if args.warmup < 3:
