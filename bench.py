@@ -281,14 +281,15 @@ class StepStats:
         self.d2h += st["d2h_bytes"]
 
 
-def learned_step(e, b, algo, limit, acc, use_graph):
+def learned_step(e, b, algo, limit, acc, use_graph, knobs):
     """One batch in learned order; queries over the work limit run again in
     heuristic order (the fallback).  Returns (results, fallbacks)."""
-    rs = e.match_batch(b, algo=algo, order_source=F.ORDER_LEARNED, max_work=limit, use_graph=use_graph)
+    rs = e.match_batch(b, algo=algo, order_source=F.ORDER_LEARNED, max_work=limit, use_graph=use_graph, **knobs)
     acc.add(e.last_stats())
     redo = [i for i, r in enumerate(rs) if r.status == F.ELIMIT]
     if redo:
-        again = e.match_batch([b[i] for i in redo], algo=algo, order_source=F.ORDER_HEURISTIC, use_graph=use_graph)
+        again = e.match_batch([b[i] for i in redo], algo=algo, order_source=F.ORDER_HEURISTIC, use_graph=use_graph,
+                              **knobs)
         acc.add(e.last_stats())
         for i, r in zip(redo, again):
             rs[i] = r
@@ -309,11 +310,21 @@ def run_ours(args, dist):
         limit = args.max_work or (WORK_BUDGET if order == "learned" else 0)
 
         use_graph = not args.no_graph
+        knobs, tune_note = {}, "defaults"
+        if not args.no_autotune:
+            from fsig_gb300 import autotune
+            t = time.time()
+            osrc = F.ORDER_LEARNED if order == "learned" else F.ORDER_HEURISTIC
+            knobs, trials = autotune.tune(e, batches[-1], algo=algo, order_source=osrc, max_work=limit,
+                                          use_graph=use_graph)
+            tune_note = f"coordinate descent on the last batch, {len(trials)} trials, {time.time() - t:.1f}s"
+            log(f"[bench] autotuned {knobs} ({tune_note})")
 
         def step(b, acc):
             if order == "learned":
-                return learned_step(e, b, algo, limit, acc, use_graph)
-            rs = e.match_batch(b, algo=algo, order_source=F.ORDER_HEURISTIC, max_work=limit, use_graph=use_graph)
+                return learned_step(e, b, algo, limit, acc, use_graph, knobs)
+            rs = e.match_batch(b, algo=algo, order_source=F.ORDER_HEURISTIC, max_work=limit, use_graph=use_graph,
+                               **knobs)
             acc.add(e.last_stats())
             return rs, 0
 
@@ -349,7 +360,7 @@ def run_ours(args, dist):
         identical = True
         for k in range(args.steps):
             b = batches[k % len(batches)]
-            rs = e.match_batch(b, algo=algo, order_source=F.ORDER_HEURISTIC, use_graph=use_graph)
+            rs = e.match_batch(b, algo=algo, order_source=F.ORDER_HEURISTIC, use_graph=use_graph, **knobs)
             heur.add(e.last_stats())
             identical &= [(r.count, r.hash) for r in rs] == results[k]
         dev_ms, enum_ms, enum_bytes = acc.dev_ms, acc.enum_ms, acc.enum_bytes
@@ -388,7 +399,8 @@ def run_ours(args, dist):
                    "algo": args.algo, "order": order, "parallelism": f"replicas x{dist.world}, queries sharded",
                    "l2": "inputs larger than L2 (resident graph arrays > 129 MB)" if args.workload in ("c5",) else
                    "graph fits L2; batches differ step to step",
-                   "work_limit": limit, "cuda_graph": use_graph, "queries_over_limit": over, "learned_fallbacks": fallbacks,
+                   "work_limit": limit, "cuda_graph": use_graph, "knobs": knobs or "defaults",
+                   "autotune": tune_note, "queries_over_limit": over, "learned_fallbacks": fallbacks,
                    "selection": f"first queries of a seeded random-walk sequence whose enumeration examines at most "
                                 f"{WORK_BUDGET} driver entries"},
         "e2e": {"value": round(tot_q / wall_s, 3), "unit": "queries/s",
@@ -476,6 +488,7 @@ def main():
     ap.add_argument("--ref-step-s", type=float, default=8.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-graph", action="store_true", help="ordinary launches instead of one CUDA graph per batch")
+    ap.add_argument("--no-autotune", action="store_true", help="default launch knobs instead of autotuned ones")
     ap.add_argument("--single-sample", type=int, default=64)
     args = ap.parse_args()
     if args.warmup < 3:

@@ -1,0 +1,71 @@
+"""Autotuner of the batched path's launch knobs, by measurement.
+
+The enumeration kernel's behaviour on a workload depends on four knobs of
+``fsig_batch_opts``:
+
+* ``warps_per_block`` - block size of the persistent enumeration launch
+  (warps that share an SM's blocks);
+* ``chunk`` - tasks a warp takes per grab of the shared task counter;
+* ``split_len`` - driver entries per task range (the unit of root tasks and
+  hand-offs, and so of load balance);
+* ``split_cycles`` - SM cycles a task runs before its unexplored frontier may
+  be handed to idle warps.
+
+The set-intersection strategy needs no knob: the kernel picks per driver
+window between the warp-cooperative 32-ary window search and per-lane binary
+search from the list-length ratio.
+
+``tune`` runs coordinate descent over a small grid on a sample batch: one knob
+at a time, each value timed by device time (CUDA events of the engine) as the
+median of ``repeats`` runs, keeping the best before moving to the next knob.
+Every trial's counts and hashes must equal the first run's; a knob choice
+never changes results, so a mismatch is an engine fault and raises.
+"""
+from __future__ import annotations
+
+import statistics
+from typing import Sequence
+
+from . import ALGO_FUSED, ORDER_HEURISTIC, Engine, Query
+
+GRID = {
+    "warps_per_block": [4, 8],
+    "chunk": [1, 2, 4, 8],
+    "split_len": [64, 128, 256, 512, 1024],
+    "split_cycles": [1000, 4000, 16000, 64000],
+}
+DEFAULTS = {"warps_per_block": 8, "chunk": 4, "split_len": 256, "split_cycles": 4000}
+
+
+def _time(engine: Engine, batch, kw, repeats: int, want):
+    ts = []
+    for _ in range(repeats):
+        rs = engine.match_batch(batch, **kw)
+        got = [(r.count, r.hash) for r in rs]
+        if want is not None and got != want:
+            raise RuntimeError(f"launch knobs {kw} changed the results")
+        st = engine.last_stats()
+        ts.append(st["ms_filter"] + st["ms_join"])
+    return statistics.median(ts), got
+
+
+def tune(engine: Engine, batch: Sequence[Query], algo: int = ALGO_FUSED, order_source: int = ORDER_HEURISTIC,
+         repeats: int = 2, rounds: int = 1, **fixed):
+    """Best knobs for the batch: (dict of knobs, list of (knobs, ms) trials).
+    `fixed` (e.g. max_work, use_graph) is passed to every run unchanged."""
+    base = dict(algo=algo, order_source=order_source, **fixed)
+    best = dict(DEFAULTS)
+    engine.match_batch(batch, **base, **best)  # warm-up
+    best_ms, want = _time(engine, batch, {**base, **best}, repeats, None)
+    trials = [(dict(best), best_ms)]
+    for _ in range(rounds):
+        for knob, values in GRID.items():
+            for v in values:
+                if v == best[knob]:
+                    continue
+                cand = dict(best, **{knob: v})
+                ms, _ = _time(engine, batch, {**base, **cand}, repeats, want)
+                trials.append((cand, ms))
+                if ms < best_ms:
+                    best, best_ms = cand, ms
+    return best, trials

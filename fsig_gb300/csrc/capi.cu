@@ -328,7 +328,7 @@ int fsig_match_batch(fsig_engine* h, uint32_t nq, const fsig_query* qs, const fs
   int rc = select(h);
   if (rc) return finish(h, rc);
   if ((nq && (!qs || !out))) return finish(h, fsig::fail(FSIG_EINVAL, "null argument"));
-  fsig_batch_opts def{FSIG_ALGO_FUSED, FSIG_ORDER_HEURISTIC, -1, 0, 0, 0, 0, 0};
+  fsig_batch_opts def{FSIG_ALGO_FUSED, FSIG_ORDER_HEURISTIC, -1, 0, 0, 0, 0, 0, 0, 0};
   const fsig_batch_opts& bo = opts ? *opts : def;
   if (bo.algo != FSIG_ALGO_FSIG && bo.algo != FSIG_ALGO_GSI && bo.algo != FSIG_ALGO_FUSED)
     return finish(h, fsig::fail(FSIG_EINVAL, "unknown algorithm"));
@@ -352,6 +352,10 @@ int fsig_match_batch(fsig_engine* h, uint32_t nq, const fsig_query* qs, const fs
     o.learned = true;
   }
   o.use_graph = bo.use_graph != 0;
+  if (bo.warps_per_block) {
+    if (bo.warps_per_block > 8) return finish(h, fsig::fail(FSIG_EINVAL, "warps_per_block must be 1..8"));
+    o.warps_per_block = bo.warps_per_block;
+  }
   if (bo.chunk) o.chunk = bo.chunk;
   if (bo.split_len) o.split = bo.split_len;
   if (bo.split_cycles) o.budget_cycles = (long long)bo.split_cycles;

@@ -95,6 +95,8 @@ typedef struct {
                             FSIG_ELIMIT.  The outcome does not depend on
                             scheduling: it is set iff the query's total work
                             under its order exceeds the limit (0: no limit)     */
+  uint32_t warps_per_block; /* enumeration block size in warps, 1..8 (0: default 8) */
+  uint32_t reserved;
 } fsig_batch_opts;
 
 /* ---- engine lifetime; replaces GPUSubgraphMatcher::init_GPU (match/subgraph_match.h:51-80)
