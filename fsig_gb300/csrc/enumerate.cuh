@@ -125,7 +125,7 @@ __device__ __forceinline__ uint32_t warp_lower_bound(const uint32_t* __restrict_
   return lo + __popc(__ballot_sync(kFull, in && v < key));
 }
 
-__global__ void __launch_bounds__(256) enumerate_kernel(EnumArgs A) {
+__global__ void __launch_bounds__(256, 4) enumerate_kernel(EnumArgs A) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   WarpSmem& ws = reinterpret_cast<WarpSmem*>(smem_raw)[threadIdx.x >> 5];
   const uint32_t lane = threadIdx.x & 31;
@@ -215,8 +215,12 @@ __global__ void __launch_bounds__(256) enumerate_kernel(EnumArgs A) {
   };
 
   // Examines the next 32 driver entries of depth lv.  x: candidate (new id);
-  // xo (leaf only): its caller id.
-  auto examine = [&](uint32_t lv, bool leaf, uint32_t& x, uint32_t& xo) -> bool {
+  // xo (leaf only): its caller id.  At the leaf depth the driver windows are
+  // examined in ascending order without leaving the depth, so lane j keeps in
+  // cur the position in backward segment j below which no later window's
+  // entries can lie (the end of the last window found there), and searches
+  // from it, first within the 32 entries that follow it.
+  auto examine = [&](uint32_t lv, bool leaf, uint32_t& x, uint32_t& xo, uint32_t& cur) -> bool {
     const uint32_t dp = __shfl_sync(kFull, dpos, lv), de = __shfl_sync(kFull, dend, lv);
     const uint32_t dv = __shfl_sync(kFull, drv, lv);
     const int32_t lab = ws.plan.lab[lv];
@@ -250,14 +254,52 @@ __global__ void __launch_bounds__(256) enumerate_kernel(EnumArgs A) {
     }
     if (bw) {
       const uint32_t xfirst = __shfl_sync(kFull, x, 0), xlast = __shfl_sync(kFull, x, nvalid - 1);
+      if (leaf) my_lo = max(my_lo, cur);
       while (bw) {
         const uint32_t j = __ffs(bw) - 1;
         bw &= bw - 1;
         const uint32_t lo = __shfl_sync(kFull, my_lo, j), hi = __shfl_sync(kFull, my_hi, j);
-        const uint32_t a = warp_lower_bound(g.adj, lo, hi, xfirst, lane, bytes);
-        const uint32_t b = warp_lower_bound(g.adj, a, hi, xlast + 1, lane, bytes);
+        uint32_t a, b;
+        bool have = false;
+        if (leaf) {
+          // the 32 entries after the cursor hold the window when it is near
+          const uint32_t idx = lo + lane;
+          const uint32_t v = idx < hi ? __ldg(g.adj + idx) : 0xffffffffu;
+          if (idx < hi) bytes += 4;
+          const uint32_t ta = __popc(__ballot_sync(kFull, v < xfirst));
+          const uint32_t tb = __popc(__ballot_sync(kFull, v <= xlast));
+          const bool ends = lo + 32 >= hi;
+          if (tb < 32 || ends) {
+            // window [lo + ta, lo + tb) lies in this tile: shuffle search
+            a = lo + ta;
+            b = lo + tb;
+            uint32_t l2 = ta, h2 = tb;
+#pragma unroll
+            for (int step = 0; step < 6; step++) {
+              const uint32_t mid = (l2 + h2) >> 1;
+              const uint32_t y = __shfl_sync(kFull, v, mid & 31);
+              if (l2 < h2) {
+                if (y < x) l2 = mid + 1; else h2 = mid;
+              }
+            }
+            const uint32_t y = __shfl_sync(kFull, v, l2 & 31);
+            pred = pred && l2 < tb && y == x;
+            have = true;
+          } else if (ta < 32) {
+            a = lo + ta;
+            b = warp_lower_bound(g.adj, lo + 32, hi, xlast + 1, lane, bytes);
+          } else {
+            a = warp_lower_bound(g.adj, lo + 32, hi, xfirst, lane, bytes);
+            b = warp_lower_bound(g.adj, a, hi, xlast + 1, lane, bytes);
+          }
+          if (lane == j) cur = b;
+        } else {
+          a = warp_lower_bound(g.adj, lo, hi, xfirst, lane, bytes);
+          b = warp_lower_bound(g.adj, a, hi, xlast + 1, lane, bytes);
+        }
         const uint32_t w = b - a;
-        if (w == 0) {
+        if (have) {
+        } else if (w == 0) {
           pred = false;
         } else if (w <= 32) {
           const uint32_t tile = lane < w ? __ldg(g.adj + a + lane) : 0xffffffffu;
@@ -423,9 +465,10 @@ __global__ void __launch_bounds__(256) enumerate_kernel(EnumArgs A) {
       if (lv == n - 1) {
         const unsigned long long Sp = __shfl_sync(kFull, S, lv - 1);
         const uint64_t tb = uint64_t(ws.plan.qv[lv]) << 32;
+        uint32_t leaf_cur = 0;  // lane j: search start in backward segment j
         while (__shfl_sync(kFull, dpos, lv) < __shfl_sync(kFull, dend, lv)) {
           uint32_t x, xo;
-          const bool p = examine(lv, true, x, xo);
+          const bool p = examine(lv, true, x, xo, leaf_cur);
           const uint32_t m = __ballot_sync(kFull, p);
           if (p) {
             my_count += 1;
@@ -458,7 +501,8 @@ __global__ void __launch_bounds__(256) enumerate_kernel(EnumArgs A) {
       }
       if (__shfl_sync(kFull, dpos, lv) < __shfl_sync(kFull, dend, lv)) {
         uint32_t x, xo;
-        const bool p = examine(lv, false, x, xo);
+        uint32_t no_cur = 0;
+        const bool p = examine(lv, false, x, xo, no_cur);
         const uint32_t m = __ballot_sync(kFull, p);
         __syncwarp();
         if (p) ws.cand[lv][__popc(m & lanemask_lt())] = x;
