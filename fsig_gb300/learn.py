@@ -285,8 +285,8 @@ def training_workloads():
     mixed = [(int(n), QUERY_DENSE if i % 2 else QUERY_SPARSE, 70_000_000 + i, 4)
              for i, n in enumerate(rng.integers(4, 33, 3000))]
     eight = [(8, QUERY_DENSE if i % 2 else QUERY_SPARSE, 71_000_000 + i, 4) for i in range(600)]
-    five = [(5, QUERY_INDUCED, 72_000_000 + i) for i in range(96)]
-    return [("chung-lu 320k", chung_lu, mixed + eight, 1 << 26), ("r-mat 2^20 unlabeled", rmat, five, 1 << 28)]
+    five = [(5, QUERY_INDUCED, 72_000_000 + i) for i in range(64)]
+    return [("chung-lu 320k", chung_lu, mixed + eight, 1 << 25), ("r-mat 2^20 unlabeled", rmat, five, 1 << 26)]
 
 
 def main(argv=None):
@@ -312,6 +312,8 @@ def main(argv=None):
             csr = g.csr()
             e.load_graph(g)
             qs = select_within_budget(e, gen_queries(g, specs, csr=csr), len(specs), args.work_limit or limit)
+            print(f"[learn] {name}: {len(qs)} of {len(specs)} queries within the work limit, "
+                  f"{time.time() - t0:.1f}s", flush=True)
             lg = collect_logs(e, qs, per_query=args.per_query, seed=args.seed)
             gain = sum(x.heuristic_work for x in lg) / max(sum(x.best[1] for x in lg), 1)
             print(f"[learn] {name}: {len(lg)} queries logged, best/heuristic total work 1/{gain:.3f}, "
