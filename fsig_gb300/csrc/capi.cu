@@ -152,6 +152,10 @@ int fsig_create(int device, uint64_t arena_bytes, fsig_engine** out) {
     err = cudaEventCreate(&ev);
     if (err != cudaSuccess) return bail(fsig::fail_cuda(err, "cudaEventCreate", __FILE__, __LINE__));
   }
+  for (auto& ev : e.ev_outer) {
+    err = cudaEventCreate(&ev);
+    if (err != cudaSuccess) return bail(fsig::fail_cuda(err, "cudaEventCreate", __FILE__, __LINE__));
+  }
   uint64_t bytes = arena_bytes ? arena_bytes : uint64_t(prop.totalGlobalMem) / 4;
   err = cudaMalloc(&e.arena.base, bytes);
   if (err != cudaSuccess) return bail(fsig::fail(FSIG_EADMISSION, "cannot reserve the device arena"));
@@ -168,6 +172,8 @@ int fsig_destroy(fsig_engine* h) {
   for (auto& ev : h->e.ev)
     if (ev) cudaEventDestroy(ev);
   for (auto& ev : h->e.ev_enum)
+    if (ev) cudaEventDestroy(ev);
+  for (auto& ev : h->e.ev_outer)
     if (ev) cudaEventDestroy(ev);
   fsig::mpnn_free(h->e);
   if (h->e.gexec) cudaGraphExecDestroy(h->e.gexec);

@@ -50,6 +50,7 @@ struct Engine {
   // timing events
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   cudaEvent_t ev_enum[2] = {nullptr, nullptr};
+  cudaEvent_t ev_outer[2] = {nullptr, nullptr};  // around a graph launch
   fsig_batch_stats last{};
   uint64_t cur_h2d = 0;  // host-to-device bytes of the call in progress
   unsigned long long last_ev[8] = {0};  // enumeration event counters of the last call

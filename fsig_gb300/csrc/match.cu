@@ -540,6 +540,27 @@ int filter_stage(Engine& e, const BatchLayout& b, uint32_t mode, int refine_iter
 namespace {
 constexpr uint32_t kOverflowCap = 1u << 20;  // task records per overflow queue
 
+// Records ev on s.  Inside a stream capture an ordinary record only orders
+// the capture; the external form makes it a node of the graph.
+cudaError_t record(cudaEvent_t ev, cudaStream_t s) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  const cudaError_t err = cudaStreamIsCapturing(s, &cs);
+  if (err != cudaSuccess) return err;
+  return cs == cudaStreamCaptureStatusActive ? cudaEventRecordWithFlags(ev, s, cudaEventRecordExternal)
+                                             : cudaEventRecord(ev, s);
+}
+
+// Milliseconds between two recorded events, or -1 when the runtime cannot
+// time them (the error is cleared so that no later call reports it).
+float elapsed(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0.f;
+  if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) {
+    cudaGetLastError();
+    return -1.f;
+  }
+  return ms;
+}
+
 __global__ void ctr_init_kernel(uint32_t* ctr, uint32_t first_task, uint32_t active) {
   for (uint32_t i = threadIdx.x; i < 8 * kCtrStride; i += blockDim.x)
     ctr[i] = i == 0 ? first_task : (i == 5 * kCtrStride ? active : 0u);
@@ -558,6 +579,7 @@ struct EnumRun {
   uint32_t* h_ctr = nullptr;  // pinned, 4 counters kCtrStride apart
   uint32_t grid = 0, block = 0, active = 0, first_task = 0, pass = 0;
   size_t smem = 0;
+  bool timed = true;  // every pass's kernel time was measured
 };
 
 // One-time kernel attributes and occupancy (host calls, kept out of captures).
@@ -636,10 +658,10 @@ int enum_launch(Engine& e, EnumRun& R) {
   R.A.tag = R.pass + 1;
   ctr_init_kernel<<<1, 256, 0, s>>>(R.ctr, R.pass == 0 ? R.first_task : 0u, R.active);
   FSIG_CUDA_TRY(cudaGetLastError());
-  FSIG_CUDA_TRY(cudaEventRecord(e.ev_enum[0], s));
+  FSIG_CUDA_TRY(record(e.ev_enum[0], s));
   enumerate_kernel<<<R.grid, R.block, R.smem, s>>>(R.A);
   FSIG_CUDA_TRY(cudaGetLastError());
-  FSIG_CUDA_TRY(cudaEventRecord(e.ev_enum[1], s));
+  FSIG_CUDA_TRY(record(e.ev_enum[1], s));
   FSIG_CUDA_TRY(cudaMemcpyAsync(R.h_ctr, R.ctr, sizeof(uint32_t) * 4 * kCtrStride, cudaMemcpyDeviceToHost, s));
   return FSIG_OK;
 }
@@ -647,9 +669,9 @@ int enum_launch(Engine& e, EnumRun& R) {
 // Call once the stream has passed the pass's counter copy.  Sets more when
 // records are left for another pass, and readies that pass.
 int enum_after(Engine& e, EnumRun& R, bool& more, float& ms_enum, uint64_t& d2h) {
-  float ms = 0;
-  FSIG_CUDA_TRY(cudaEventElapsedTime(&ms, e.ev_enum[0], e.ev_enum[1]));
-  ms_enum += ms;
+  const float ms = elapsed(e.ev_enum[0], e.ev_enum[1]);
+  if (ms < 0.f) R.timed = false;
+  else ms_enum += ms;
   d2h += sizeof(uint32_t) * 4 * kCtrStride;
   const uint32_t* hc = R.h_ctr;
   if (hc[3 * kCtrStride] & kErrTimeout) return fail(FSIG_ETIMEOUT, "a work-queue record was not published in time");
@@ -770,7 +792,7 @@ int run_batch(Engine& e, const std::vector<HostQuery>& qs, const BatchOptions& o
   // Everything from the uploads to the results' copy back, in stream order.
   auto enqueue = [&]() -> int {
     int rc = FSIG_OK;
-    FSIG_CUDA_TRY(cudaEventRecord(e.ev[0], s));
+    FSIG_CUDA_TRY(record(e.ev[0], s));
     QVert* d_qv = stage_upload(e, st, b.qv, rc);
     if (rc) return rc;
     uint32_t* d_qoff = stage_upload(e, st, b.qoff, rc);
@@ -806,7 +828,7 @@ int run_batch(Engine& e, const std::vector<HostQuery>& qs, const BatchOptions& o
     rc = filter_stage(e, b, opt.filter_mode, opt.refine_iters, d_qv, d_gword, d_lab_gidx, d_lab_begin, pool,
                       d_counts, &launches);
     if (rc) return rc;
-    FSIG_CUDA_TRY(cudaEventRecord(e.ev[1], s));
+    FSIG_CUDA_TRY(record(e.ev[1], s));
 
     uint32_t order_mode = opt.order_mode;
     if (opt.host_order) {
@@ -895,7 +917,7 @@ int run_batch(Engine& e, const std::vector<HostQuery>& qs, const BatchOptions& o
   };
   // The results' copy back (after the last pass).
   auto copy_back = [&]() -> int {
-    FSIG_CUDA_TRY(cudaEventRecord(e.ev[2], s));
+    FSIG_CUDA_TRY(record(e.ev[2], s));
     FSIG_CUDA_TRY(cudaMemcpyAsync(h_res, d_res, sizeof(QueryResult) * Q, cudaMemcpyDeviceToHost, s));
     FSIG_CUDA_TRY(cudaMemcpyAsync(h_counts, d_counts, sizeof(uint32_t) * b.G, cudaMemcpyDeviceToHost, s));
     FSIG_CUDA_TRY(cudaMemcpyAsync(h_orders, d_orders, sizeof(uint32_t) * Q * kMaxQ, cudaMemcpyDeviceToHost, s));
@@ -934,7 +956,9 @@ int run_batch(Engine& e, const std::vector<HostQuery>& qs, const BatchOptions& o
       }
     }
     cudaGraphDestroy(cg);
+    FSIG_CUDA_TRY(cudaEventRecord(e.ev_outer[0], s));
     FSIG_CUDA_TRY(cudaGraphLaunch(e.gexec, s));
+    FSIG_CUDA_TRY(cudaEventRecord(e.ev_outer[1], s));
     FSIG_CUDA_TRY(cudaStreamSynchronize(s));
     out.passes = 1;
     rc = enum_after(e, R, more, out.ms_enum, d2h);
@@ -950,6 +974,7 @@ int run_batch(Engine& e, const std::vector<HostQuery>& qs, const BatchOptions& o
       }
       rc = copy_back();
       if (rc) return rc;
+      FSIG_CUDA_TRY(cudaEventRecord(e.ev_outer[1], s));
       FSIG_CUDA_TRY(cudaStreamSynchronize(s));
     }
   } else {
@@ -990,8 +1015,14 @@ int run_batch(Engine& e, const std::vector<HostQuery>& qs, const BatchOptions& o
   std::memcpy(e.last_ev, h_ev, sizeof(e.last_ev));
   out.algo_bytes = *h_misc;
   for (uint32_t q = 0; q < Q; q++) out.ok[q] = h_plans[q].ok;
-  FSIG_CUDA_TRY(cudaEventElapsedTime(&out.ms_filter, e.ev[0], e.ev[1]));
-  FSIG_CUDA_TRY(cudaEventElapsedTime(&out.ms_join, e.ev[1], e.ev[2]));
+  out.ms_filter = elapsed(e.ev[0], e.ev[1]);
+  out.ms_join = elapsed(e.ev[1], e.ev[2]);
+  if (out.ms_filter < 0.f || out.ms_join < 0.f) {
+    // the phases inside the graph could not be timed: the whole launch counts as join
+    out.ms_filter = 0.f;
+    out.ms_join = graph ? std::max(elapsed(e.ev_outer[0], e.ev_outer[1]), 0.f) : 0.f;
+  }
+  if (!R.timed) out.ms_enum = -1.f;
   d2h += sizeof(QueryResult) * Q + sizeof(uint32_t) * b.G + sizeof(uint32_t) * Q * kMaxQ +
          sizeof(unsigned long long) + sizeof(Plan) * Q + sizeof(e.last_ev);
   out.h2d_bytes = e.cur_h2d;

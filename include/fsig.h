@@ -190,7 +190,8 @@ typedef struct {
   uint32_t enum_passes;      /* enumeration kernel launches (work-splitting passes) */
   float ms_filter;           /* device time, filter + refinement + counts       */
   float ms_join;             /* device time, ordering + roots + enumeration     */
-  float ms_enum;             /* device time of the enumeration kernel launches  */
+  float ms_enum;             /* device time of the enumeration kernel launches
+                                (-1 when a graph launch left it unmeasurable)  */
   uint32_t graph;            /* 1 when the batch ran as one CUDA graph          */
   uint64_t enum_tasks;       /* tasks run by the enumeration kernel             */
   uint64_t enum_pops;        /* handed-off records taken within the same pass   */
