@@ -20,7 +20,9 @@ def test_autotune_on_a_small_batch(engine):
     best, trials = autotune.tune(engine, qs, repeats=1, use_graph=True)
     assert set(best) == set(autotune.GRID)
     assert all(best[k] in autotune.GRID[k] for k in best)
-    assert len(trials) == 1 + sum(len(v) - 1 for v in autotune.GRID.values())
+    # every grid value is tried once per knob (the starting value again when
+    # an earlier value of the same knob displaced it)
+    assert 1 + sum(len(v) - 1 for v in autotune.GRID.values()) <= len(trials) <= 1 + sum(map(len, autotune.GRID.values()))
     assert [(r.count, r.hash) for r in engine.match_batch(qs, **best)] == base
     for wpb in (1, 2, 4):
         assert [(r.count, r.hash) for r in engine.match_batch(qs, warps_per_block=wpb)] == base
