@@ -83,9 +83,16 @@ constexpr uint32_t kMaxWaiters = 2048;     // warps beyond this many idle ones l
 constexpr uint32_t kReadySpinLimit = 1u << 22;
 constexpr uint32_t kIdleSpinLimit = 1u << 22;
 
+// Search cursors: for depth lv and backward position j < lv, the position
+// in j's segment below which no entry of a later driver window of depth lv can
+// lie (triangular layout, lv(lv-1)/2 + j).  Each lane j owns its slots.
+constexpr uint32_t kCursors = kMaxQ * (kMaxQ - 1) / 2;
+__device__ __forceinline__ uint32_t cursor_base(uint32_t lv) { return lv * (lv - 1) / 2; }
+
 struct WarpSmem {
   Plan plan;
   uint32_t cand[kMaxQ][kChunk];
+  uint32_t cur[kCursors];
 };
 
 __device__ __forceinline__ bool bsearch_range(const uint32_t* __restrict__ a, uint32_t lo, uint32_t hi, uint32_t x,
@@ -212,23 +219,25 @@ __global__ void __launch_bounds__(256, 4) enumerate_kernel(EnumArgs A) {
       cnt = 0;
       it = 0;
     }
+    if (lane < lv) ws.cur[cursor_base(lv) + lane] = 0u;  // a new driver scan of depth lv
   };
 
   // Examines the next 32 driver entries of depth lv.  x: candidate (new id);
-  // xo (leaf only): its caller id.  At the leaf depth the driver windows are
-  // examined in ascending order without leaving the depth, so lane j keeps in
-  // cur the position in backward segment j below which no later window's
-  // entries can lie (the end of the last window found there), and searches
-  // from it, first within the 32 entries that follow it.
-  auto examine = [&](uint32_t lv, bool leaf, uint32_t& x, uint32_t& xo, uint32_t& cur) -> bool {
+  // xo (leaf only): its caller id.  The driver windows of a depth are
+  // examined in ascending order, so each backward segment is searched from
+  // its cursor (the end of the last window found there); when the segment's
+  // rest is about as long as the driver's, the window usually lies in the 32
+  // entries after the cursor and one coalesced load finds it.
+  auto examine = [&](uint32_t lv, bool leaf, uint32_t& x, uint32_t& xo) -> bool {
     const uint32_t dp = __shfl_sync(kFull, dpos, lv), de = __shfl_sync(kFull, dend, lv);
     const uint32_t dv = __shfl_sync(kFull, drv, lv);
     const int32_t lab = ws.plan.lab[lv];
     uint32_t bw = ws.plan.bwd[lv] & ~(1u << dv);
     uint32_t my_lo = 0, my_hi = 0;
+    uint32_t* cur = ws.cur + cursor_base(lv);
     if ((bw >> lane) & 1u) {
       const uint32_t* s = g.lseg + uint64_t(f) * W1 + lab;
-      my_lo = s[0];
+      my_lo = max(s[0], cur[lane]);
       my_hi = s[1];
       bytes += 8;
     }
@@ -254,14 +263,14 @@ __global__ void __launch_bounds__(256, 4) enumerate_kernel(EnumArgs A) {
     }
     if (bw) {
       const uint32_t xfirst = __shfl_sync(kFull, x, 0), xlast = __shfl_sync(kFull, x, nvalid - 1);
-      if (leaf) my_lo = max(my_lo, cur);
+      const uint32_t rem = de - dp;  // driver entries left at this depth
       while (bw) {
         const uint32_t j = __ffs(bw) - 1;
         bw &= bw - 1;
         const uint32_t lo = __shfl_sync(kFull, my_lo, j), hi = __shfl_sync(kFull, my_hi, j);
         uint32_t a, b;
         bool have = false;
-        if (leaf) {
+        if (hi - lo <= rem + 32) {
           // the 32 entries after the cursor hold the window when it is near
           const uint32_t idx = lo + lane;
           const uint32_t v = idx < hi ? __ldg(g.adj + idx) : 0xffffffffu;
@@ -292,11 +301,11 @@ __global__ void __launch_bounds__(256, 4) enumerate_kernel(EnumArgs A) {
             a = warp_lower_bound(g.adj, lo + 32, hi, xfirst, lane, bytes);
             b = warp_lower_bound(g.adj, a, hi, xlast + 1, lane, bytes);
           }
-          if (lane == j) cur = b;
         } else {
           a = warp_lower_bound(g.adj, lo, hi, xfirst, lane, bytes);
           b = warp_lower_bound(g.adj, a, hi, xlast + 1, lane, bytes);
         }
+        if (lane == j) cur[j] = b;
         const uint32_t w = b - a;
         if (have) {
         } else if (w == 0) {
@@ -465,10 +474,9 @@ __global__ void __launch_bounds__(256, 4) enumerate_kernel(EnumArgs A) {
       if (lv == n - 1) {
         const unsigned long long Sp = __shfl_sync(kFull, S, lv - 1);
         const uint64_t tb = uint64_t(ws.plan.qv[lv]) << 32;
-        uint32_t leaf_cur = 0;  // lane j: search start in backward segment j
         while (__shfl_sync(kFull, dpos, lv) < __shfl_sync(kFull, dend, lv)) {
           uint32_t x, xo;
-          const bool p = examine(lv, true, x, xo, leaf_cur);
+          const bool p = examine(lv, true, x, xo);
           const uint32_t m = __ballot_sync(kFull, p);
           if (p) {
             my_count += 1;
@@ -501,8 +509,7 @@ __global__ void __launch_bounds__(256, 4) enumerate_kernel(EnumArgs A) {
       }
       if (__shfl_sync(kFull, dpos, lv) < __shfl_sync(kFull, dend, lv)) {
         uint32_t x, xo;
-        uint32_t no_cur = 0;
-        const bool p = examine(lv, false, x, xo, no_cur);
+        const bool p = examine(lv, false, x, xo);
         const uint32_t m = __ballot_sync(kFull, p);
         __syncwarp();
         if (p) ws.cand[lv][__popc(m & lanemask_lt())] = x;
