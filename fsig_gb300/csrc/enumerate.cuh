@@ -247,12 +247,13 @@ __global__ void __launch_bounds__(256, 4) enumerate_kernel(EnumArgs A) {
     x = pred ? __ldg(g.adj + k) : 0xffffffffu;
     xo = (pred && leaf) ? __ldg(g.adj_old + k) : 0u;
     if (pred) bytes += leaf ? 8 : 4;
-    // candidate bitmap of depth lv, issued before the window searches
-    uint32_t bmw = 0;
-    const uint32_t bit = x - ws.plan.bmbase[lv];
+    // the depth's candidate bitmap and injectivity first: entries they reject
+    // need no segment search, and a window they empty needs none at all
     if (pred) {
-      bmw = __ldg(A.pool + ws.plan.bmoff[lv] + (bit >> 5));
+      const uint32_t bit = x - ws.plan.bmbase[lv];
+      const uint32_t bmw = __ldg(A.pool + ws.plan.bmoff[lv] + (bit >> 5));
       bytes += 4;
+      pred = (bmw >> (bit & 31)) & 1u;
     }
     uint32_t sm = ws.plan.same[lv];
     while (sm) {
@@ -261,8 +262,11 @@ __global__ void __launch_bounds__(256, 4) enumerate_kernel(EnumArgs A) {
       const uint32_t fj = __shfl_sync(kFull, f, j);
       pred = pred && x != fj;
     }
-    if (bw) {
-      const uint32_t xfirst = __shfl_sync(kFull, x, 0), xlast = __shfl_sync(kFull, x, nvalid - 1);
+    const uint32_t alive = __ballot_sync(kFull, pred);
+    if (bw && alive) {
+      // searched window: from the first to the last surviving entry
+      const uint32_t xfirst = __shfl_sync(kFull, x, __ffs(alive) - 1);
+      const uint32_t xlast = __shfl_sync(kFull, x, 31 - __clz(alive));
       const uint32_t rem = de - dp;  // driver entries left at this depth
       while (bw) {
         const uint32_t j = __ffs(bw) - 1;
@@ -283,8 +287,7 @@ __global__ void __launch_bounds__(256, 4) enumerate_kernel(EnumArgs A) {
             a = lo + ta;
             b = lo + tb;
             uint32_t l2 = ta, h2 = tb;
-#pragma unroll
-            for (int step = 0; step < 6; step++) {
+            for (uint32_t steps = 32 - __clz(tb - ta); steps; steps--) {  // bit length of the window
               const uint32_t mid = (l2 + h2) >> 1;
               const uint32_t y = __shfl_sync(kFull, v, mid & 31);
               if (l2 < h2) {
@@ -314,8 +317,7 @@ __global__ void __launch_bounds__(256, 4) enumerate_kernel(EnumArgs A) {
           const uint32_t tile = lane < w ? __ldg(g.adj + a + lane) : 0xffffffffu;
           bytes += lane < w ? 4 : 0;
           uint32_t l2 = 0, h2 = w;
-#pragma unroll
-          for (int step = 0; step < 6; step++) {
+          for (uint32_t steps = 32 - __clz(w); steps; steps--) {
             const uint32_t mid = (l2 + h2) >> 1;
             const uint32_t v = __shfl_sync(kFull, tile, mid & 31);
             if (l2 < h2) {
@@ -330,7 +332,6 @@ __global__ void __launch_bounds__(256, 4) enumerate_kernel(EnumArgs A) {
         if (__ballot_sync(kFull, pred) == 0) break;
       }
     }
-    pred = pred && ((bmw >> (bit & 31)) & 1u);
     if (lane == lv) dpos = dp + kChunk;
     if (lane == 0) {
       n_examine++;
