@@ -15,8 +15,9 @@ compaction + enumeration.
 
 Order: the learned order (the packaged order-scoring network,
 fsig_gb300/order_net.npy, trained on logs of the mid-scale graphs) when it
-exists, with a per-query work limit; a query over the limit runs again in the
-heuristic order, inside the timed region.  After the timed region the same
+exists, with a per-query work limit; a query over the limit is carried into
+the next batch with its heuristic order attached (the last ones run in a batch
+of their own), inside the timed region.  After the timed region the same
 batches run in heuristic order ("heuristic_batched"), and every count and
 hash is compared between the two.  "single_query_path" is the plain
 one-query-per-call heuristic path (fsig_match) on a sample.
@@ -288,19 +289,43 @@ class StepStats:
         self.d2h += st["d2h_bytes"]
 
 
-def learned_step(e, b, algo, limit, acc, use_graph, knobs):
-    """One batch in learned order; queries over the work limit run again in
-    heuristic order (the fallback).  Returns (results, fallbacks)."""
-    rs = e.match_batch(b, algo=algo, order_source=F.ORDER_LEARNED, max_work=limit, use_graph=use_graph, **knobs)
-    acc.add(e.last_stats())
-    redo = [i for i, r in enumerate(rs) if r.status == F.ELIMIT]
-    if redo:
-        again = e.match_batch([b[i] for i in redo], algo=algo, order_source=F.ORDER_HEURISTIC, use_graph=use_graph,
-                              **knobs)
-        acc.add(e.last_stats())
-        for i, r in zip(redo, again):
-            rs[i] = r
-    return rs, len(redo)
+class LearnedFeed:
+    """Learned-order batches.  A query over the work limit (the fallback) is
+    carried into the next batch with its heuristic order attached, which a
+    learned-order batch keeps; those left after the last batch run in a batch
+    of their own at flush().  Results are written into results[step][i]."""
+
+    def __init__(self, e, algo, limit, use_graph, knobs):
+        self.e, self.algo, self.limit, self.use_graph, self.knobs = e, algo, limit, use_graph, knobs
+        self.pending = []  # (step, index, query with its heuristic order)
+
+    def _run(self, qs, acc):
+        rs = self.e.match_batch(qs, algo=self.algo, order_source=F.ORDER_LEARNED, max_work=self.limit,
+                                use_graph=self.use_graph, **self.knobs)
+        acc.add(self.e.last_stats())
+        return rs
+
+    def _settle(self, rs, results):
+        for (k, i, _), r in zip(self.pending, rs):
+            if r.status != F.OK:
+                raise RuntimeError(f"fallback query failed with status {r.status}")
+            results[k][i] = (r.count, r.hash)
+        self.pending = []
+
+    def step(self, k, b, acc, results):
+        rs = self._run(list(b) + [q for _, _, q in self.pending], acc)
+        self._settle(rs[len(b):], results)
+        rs = rs[: len(b)]
+        results[k] = [(r.count, r.hash) for r in rs]
+        for i, r in enumerate(rs):
+            if r.status == F.ELIMIT:
+                order = F.plan_order(b[i], F.ALGO_GSI, r.candidates)["order"]
+                self.pending.append((k, i, F.Query(b[i].labels, b[i].edges, order=np.asarray(order, np.uint32))))
+        return rs, sum(1 for r in rs if r.status == F.ELIMIT)
+
+    def flush(self, acc, results):
+        if self.pending:
+            self._settle(self._run([q for _, _, q in self.pending], acc), results)
 
 
 def run_ours(args, dist):
@@ -327,31 +352,34 @@ def run_ours(args, dist):
             tune_note = f"coordinate descent on the last batch, {len(trials)} trials, {time.time() - t:.1f}s"
             log(f"[bench] autotuned {knobs} ({tune_note})")
 
-        def step(b, acc):
-            if order == "learned":
-                return learned_step(e, b, algo, limit, acc, use_graph, knobs)
+        feed = LearnedFeed(e, algo, limit, use_graph, knobs) if order == "learned" else None
+
+        def step(k, b, acc, results):
+            if feed:
+                return feed.step(k, b, acc, results)
             rs = e.match_batch(b, algo=algo, order_source=F.ORDER_HEURISTIC, max_work=limit, use_graph=use_graph,
                                **knobs)
             acc.add(e.last_stats())
+            results[k] = [(r.count, r.hash) for r in rs]
             return rs, 0
 
+        warm = [None] * args.warmup
         for i in range(args.warmup):
-            step(batches[i % len(batches)], StepStats())
+            step(i, batches[i % len(batches)], StepStats(), warm)
+        if feed:
+            feed.flush(StepStats(), warm)
         dist.barrier()
         cuda_sync()
         acc = StepStats()
-        nq = emb = over = fallbacks = 0
-        results = []
+        nq = over = fallbacks = 0
+        results = [None] * args.steps
         with ClockSampler(dev) as clk:
             t0 = time.perf_counter()
             for k in range(args.steps):
                 b = batches[k % len(batches)]
                 before = acc.dev_ms
-                rs, fb = step(b, acc)
-                results.append([(r.count, r.hash) for r in rs])
+                rs, fb = step(k, b, acc, results)
                 nq += len(b)
-                emb += sum(r.count for r in rs)
-                over += sum(1 for r in rs if r.status == F.ELIMIT)
                 fallbacks += fb
                 st = e.last_stats()
                 log(f"[bench] step {k}: {len(b)} queries, {sum(r.count for r in rs)} embeddings, device "
@@ -359,9 +387,12 @@ def run_ours(args, dist):
                     f"{st['ms_filter']:.2f} ms, join {st['ms_join']:.2f} ms (enumeration {st['ms_enum']:.2f} ms, "
                     f"{st['enum_passes']} passes); tasks {st['enum_tasks']} pops {st['enum_pops']} handoffs "
                     f"{st['enum_handoffs']} records {st['enum_records']} examines {st['enum_examines']}")
+            if feed:
+                feed.flush(acc, results)
             cuda_sync()
             wall = time.perf_counter() - t0
         dist.barrier()
+        emb = sum(c for step_res in results for c, _ in step_res)
         # the same batches in heuristic order: the comparison and the bit-exactness check
         heur = StepStats()
         identical = True

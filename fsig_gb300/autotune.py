@@ -34,7 +34,7 @@ GRID = {
     "split_len": [64, 128, 256, 512, 1024],
     "split_cycles": [1000, 4000, 16000, 64000],
 }
-DEFAULTS = {"warps_per_block": 8, "chunk": 4, "split_len": 256, "split_cycles": 4000}
+DEFAULTS = {"warps_per_block": 8, "chunk": 1, "split_len": 256, "split_cycles": 4000}
 
 
 def _time(engine: Engine, batch, kw, repeats: int, want):

@@ -83,16 +83,9 @@ constexpr uint32_t kMaxWaiters = 2048;     // warps beyond this many idle ones l
 constexpr uint32_t kReadySpinLimit = 1u << 22;
 constexpr uint32_t kIdleSpinLimit = 1u << 22;
 
-// Search cursors: for depth lv and backward position j < lv, the position
-// in j's segment below which no entry of a later driver window of depth lv can
-// lie (triangular layout, lv(lv-1)/2 + j).  Each lane j owns its slots.
-constexpr uint32_t kCursors = kMaxQ * (kMaxQ - 1) / 2;
-__device__ __forceinline__ uint32_t cursor_base(uint32_t lv) { return lv * (lv - 1) / 2; }
-
 struct WarpSmem {
   Plan plan;
   uint32_t cand[kMaxQ][kChunk];
-  uint32_t cur[kCursors];
 };
 
 __device__ __forceinline__ bool bsearch_range(const uint32_t* __restrict__ a, uint32_t lo, uint32_t hi, uint32_t x,
@@ -219,25 +212,23 @@ __global__ void __launch_bounds__(256, 4) enumerate_kernel(EnumArgs A) {
       cnt = 0;
       it = 0;
     }
-    if (lane < lv) ws.cur[cursor_base(lv) + lane] = 0u;  // a new driver scan of depth lv
   };
 
   // Examines the next 32 driver entries of depth lv.  x: candidate (new id);
-  // xo (leaf only): its caller id.  The driver windows of a depth are
-  // examined in ascending order, so each backward segment is searched from
-  // its cursor (the end of the last window found there); when the segment's
-  // rest is about as long as the driver's, the window usually lies in the 32
-  // entries after the cursor and one coalesced load finds it.
-  auto examine = [&](uint32_t lv, bool leaf, uint32_t& x, uint32_t& xo) -> bool {
+  // xo (leaf only): its caller id.  At the leaf depth the driver windows are
+  // examined in ascending order without leaving the depth, so lane j keeps in
+  // cur the position in backward segment j below which no later window's
+  // entries can lie (the end of the last window found there), and searches
+  // from it, first within the 32 entries that follow it.
+  auto examine = [&](uint32_t lv, bool leaf, uint32_t& x, uint32_t& xo, uint32_t& cur) -> bool {
     const uint32_t dp = __shfl_sync(kFull, dpos, lv), de = __shfl_sync(kFull, dend, lv);
     const uint32_t dv = __shfl_sync(kFull, drv, lv);
     const int32_t lab = ws.plan.lab[lv];
     uint32_t bw = ws.plan.bwd[lv] & ~(1u << dv);
     uint32_t my_lo = 0, my_hi = 0;
-    uint32_t* cur = ws.cur + cursor_base(lv);
     if ((bw >> lane) & 1u) {
       const uint32_t* s = g.lseg + uint64_t(f) * W1 + lab;
-      my_lo = max(s[0], cur[lane]);
+      my_lo = s[0];
       my_hi = s[1];
       bytes += 8;
     }
@@ -247,8 +238,6 @@ __global__ void __launch_bounds__(256, 4) enumerate_kernel(EnumArgs A) {
     x = pred ? __ldg(g.adj + k) : 0xffffffffu;
     xo = (pred && leaf) ? __ldg(g.adj_old + k) : 0u;
     if (pred) bytes += leaf ? 8 : 4;
-    // the depth's candidate bitmap and injectivity first: entries they reject
-    // need no segment search, and a window they empty needs none at all
     if (pred) {
       const uint32_t bit = x - ws.plan.bmbase[lv];
       const uint32_t bmw = __ldg(A.pool + ws.plan.bmoff[lv] + (bit >> 5));
@@ -264,17 +253,16 @@ __global__ void __launch_bounds__(256, 4) enumerate_kernel(EnumArgs A) {
     }
     const uint32_t alive = __ballot_sync(kFull, pred);
     if (bw && alive) {
-      // searched window: from the first to the last surviving entry
       const uint32_t xfirst = __shfl_sync(kFull, x, __ffs(alive) - 1);
       const uint32_t xlast = __shfl_sync(kFull, x, 31 - __clz(alive));
-      const uint32_t rem = de - dp;  // driver entries left at this depth
+      if (leaf) my_lo = max(my_lo, cur);
       while (bw) {
         const uint32_t j = __ffs(bw) - 1;
         bw &= bw - 1;
         const uint32_t lo = __shfl_sync(kFull, my_lo, j), hi = __shfl_sync(kFull, my_hi, j);
         uint32_t a, b;
         bool have = false;
-        if (hi - lo <= rem + 32) {
+        if (leaf) {
           // the 32 entries after the cursor hold the window when it is near
           const uint32_t idx = lo + lane;
           const uint32_t v = idx < hi ? __ldg(g.adj + idx) : 0xffffffffu;
@@ -287,7 +275,8 @@ __global__ void __launch_bounds__(256, 4) enumerate_kernel(EnumArgs A) {
             a = lo + ta;
             b = lo + tb;
             uint32_t l2 = ta, h2 = tb;
-            for (uint32_t steps = 32 - __clz(tb - ta); steps; steps--) {  // bit length of the window
+#pragma unroll
+            for (int step = 0; step < 6; step++) {
               const uint32_t mid = (l2 + h2) >> 1;
               const uint32_t y = __shfl_sync(kFull, v, mid & 31);
               if (l2 < h2) {
@@ -304,11 +293,11 @@ __global__ void __launch_bounds__(256, 4) enumerate_kernel(EnumArgs A) {
             a = warp_lower_bound(g.adj, lo + 32, hi, xfirst, lane, bytes);
             b = warp_lower_bound(g.adj, a, hi, xlast + 1, lane, bytes);
           }
+          if (lane == j) cur = b;
         } else {
           a = warp_lower_bound(g.adj, lo, hi, xfirst, lane, bytes);
           b = warp_lower_bound(g.adj, a, hi, xlast + 1, lane, bytes);
         }
-        if (lane == j) cur[j] = b;
         const uint32_t w = b - a;
         if (have) {
         } else if (w == 0) {
@@ -317,7 +306,8 @@ __global__ void __launch_bounds__(256, 4) enumerate_kernel(EnumArgs A) {
           const uint32_t tile = lane < w ? __ldg(g.adj + a + lane) : 0xffffffffu;
           bytes += lane < w ? 4 : 0;
           uint32_t l2 = 0, h2 = w;
-          for (uint32_t steps = 32 - __clz(w); steps; steps--) {
+#pragma unroll
+          for (int step = 0; step < 6; step++) {
             const uint32_t mid = (l2 + h2) >> 1;
             const uint32_t v = __shfl_sync(kFull, tile, mid & 31);
             if (l2 < h2) {
@@ -475,9 +465,10 @@ __global__ void __launch_bounds__(256, 4) enumerate_kernel(EnumArgs A) {
       if (lv == n - 1) {
         const unsigned long long Sp = __shfl_sync(kFull, S, lv - 1);
         const uint64_t tb = uint64_t(ws.plan.qv[lv]) << 32;
+        uint32_t leaf_cur = 0;  // lane j: search start in backward segment j
         while (__shfl_sync(kFull, dpos, lv) < __shfl_sync(kFull, dend, lv)) {
           uint32_t x, xo;
-          const bool p = examine(lv, true, x, xo);
+          const bool p = examine(lv, true, x, xo, leaf_cur);
           const uint32_t m = __ballot_sync(kFull, p);
           if (p) {
             my_count += 1;
@@ -510,7 +501,8 @@ __global__ void __launch_bounds__(256, 4) enumerate_kernel(EnumArgs A) {
       }
       if (__shfl_sync(kFull, dpos, lv) < __shfl_sync(kFull, dend, lv)) {
         uint32_t x, xo;
-        const bool p = examine(lv, false, x, xo);
+        uint32_t no_cur = 0;
+        const bool p = examine(lv, false, x, xo, no_cur);
         const uint32_t m = __ballot_sync(kFull, p);
         __syncwarp();
         if (p) ws.cand[lv][__popc(m & lanemask_lt())] = x;

@@ -561,6 +561,18 @@ float elapsed(cudaEvent_t a, cudaEvent_t b) {
   return ms;
 }
 
+// In a learned-order batch, queries that carry their own order keep it: their
+// scores become the positions of that order (thread per query).
+__global__ void given_scores_kernel(const uint32_t* __restrict__ qoff, uint32_t Q,
+                                    const uint32_t* __restrict__ has_given, const uint32_t* __restrict__ given,
+                                    float* scores) {
+  for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < Q; q += gridDim.x * blockDim.x) {
+    if (!has_given[q]) continue;
+    const uint32_t g0 = qoff[q], n = qoff[q + 1] - g0;
+    for (uint32_t i = 0; i < n; i++) scores[g0 + given[g0 + i]] = float(i);
+  }
+}
+
 __global__ void ctr_init_kernel(uint32_t* ctr, uint32_t first_task, uint32_t active) {
   for (uint32_t i = threadIdx.x; i < 8 * kCtrStride; i += blockDim.x)
     ctr[i] = i == 0 ? first_task : (i == 5 * kCtrStride ? active : 0u);
@@ -730,7 +742,7 @@ size_t stage_bytes(const BatchLayout& b) {
   const size_t a = 256;
   const size_t Q = b.Q, G = b.G;
   return 20 * a + sizeof(QVert) * G + 4 * (Q + 1) + 4 * b.lab_gidx.size() + 4 * b.lab_begin.size() +
-         8 * b.gword.size() + 4 * G + 4 * G + sizeof(QueryResult) * Q + 4 * G + 4 * Q * kMaxQ + sizeof(Plan) * Q +
+         8 * b.gword.size() + 4 * G + 4 * G + 4 * Q + sizeof(QueryResult) * Q + 4 * G + 4 * Q * kMaxQ + sizeof(Plan) * Q +
          8 + 4 * 4 * kCtrStride + 64;
 }
 }  // namespace
@@ -769,6 +781,12 @@ int run_batch(Engine& e, const std::vector<HostQuery>& qs, const BatchOptions& o
 
   std::vector<uint32_t> given(b.G, 0);
   std::vector<float> scores(b.G, 0.f);
+  std::vector<uint32_t> has_given(Q, 0);
+  bool any_given = false;
+  for (uint32_t q = 0; q < Q; q++) {
+    has_given[q] = qs[q].has_given ? 1u : 0u;
+    any_given |= qs[q].has_given;
+  }
   for (uint32_t q = 0; q < Q; q++)
     for (uint32_t i = 0; i < qs[q].n; i++) {
       given[b.qoff[q] + i] = qs[q].has_given ? qs[q].given[i] : i;
@@ -870,6 +888,14 @@ int run_batch(Engine& e, const std::vector<HostQuery>& qs, const BatchOptions& o
       rc = mpnn_forward_device(e, Q, d_qoff, d_feat, d_nbr, d_lscores);
       if (rc) return rc;
       launches += 3;
+      if (any_given) {
+        uint32_t* d_has_given = stage_upload(e, st, has_given, rc);
+        if (rc) return rc;
+        given_scores_kernel<<<std::max<uint32_t>(1, (Q + 127) / 128), 128, 0, s>>>(d_qoff, Q, d_has_given, d_given,
+                                                                                 d_lscores);
+        FSIG_CUDA_TRY(cudaGetLastError());
+        launches++;
+      }
       d_score_src = d_lscores;
       order_mode = kOrderScores;
     }

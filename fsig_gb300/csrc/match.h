@@ -80,7 +80,7 @@ struct BatchOptions {
   uint32_t filter_mode = kFilterDegree | kFilterSignature;
   int refine_iters = 0;
   uint32_t order_mode = kOrderGSI;
-  uint32_t chunk = 4;        // tasks per grab
+  uint32_t chunk = 1;        // tasks per grab
   uint32_t split = 256;      // driver entries per task range
   long long budget_cycles = 4000;     // cycles on a task before it may be split for idle warps
   unsigned long long max_work = 0;  // per-query limit on examined driver entries (0: none)

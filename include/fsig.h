@@ -133,7 +133,9 @@ void fsig_free_graph_file(fsig_graph_file* f);
  *      i.e. MMatch::match (match/MMatch.cu:2077-2121, algo 1) and GSI::match
  *      (match/GSI.cu:329-358, algo 2), for one query. ---- */
 int fsig_match(fsig_engine* e, const fsig_query* q, int algo, fsig_result* out);
-/* Many queries against the resident data graph in one persistent launch. */
+/* Many queries against the resident data graph in one persistent launch.
+ * With order_source FSIG_ORDER_LEARNED, a query that carries an order
+ * (fsig_query.order) keeps it; the others are ordered by the network. */
 int fsig_match_batch(fsig_engine* e, uint32_t num_queries, const fsig_query* qs,
                      const fsig_batch_opts* opts, fsig_result* out);
 

@@ -143,6 +143,25 @@ def test_learned_order_results_identical(engine, golden, algo):
         assert connected_permutation(l.order, q)
 
 
+def test_learned_batch_keeps_given_orders(engine, golden):
+    """In a learned-order batch, queries that carry an order keep it."""
+    _, qs = golden_graph_and_queries(engine, golden)
+    engine.mpnn_set_params(learn.init_params(8))
+    heur = engine.match_batch(qs, algo=F.ALGO_FUSED)
+    mixed = []
+    for i, (q, h) in enumerate(zip(qs, heur)):
+        if i % 2 and q.num_vertices > 2:
+            mixed.append(F.Query(q.labels, q.edges, order=np.asarray(h.order[::-1] if learn.is_connected_order(
+                h.order[::-1], learn.adjacency_masks(q)) else h.order, np.uint32)))
+        else:
+            mixed.append(q)
+    rs = engine.match_batch(mixed, algo=F.ALGO_FUSED, order_source=F.ORDER_LEARNED)
+    for q, h, r in zip(mixed, heur, rs):
+        assert (r.count, r.hash) == (h.count, h.hash)
+        if q.order is not None:
+            assert r.order == [int(x) for x in q.order]
+
+
 def test_learned_order_needs_a_network():
     with F.Engine(0, arena_bytes=1 << 28) as e:
         e.load_graph(F.gen_rmat(1000, 4000, seed=1, labels=F.gen_labels(1000, 4, seed=1)))
