@@ -133,12 +133,13 @@ def engine_library() -> C.CDLL:
     L.fsig_read_graph_file.argtypes = [C.c_char_p, C.c_int, C.POINTER(vp)]
     L.fsig_graph_file_data.argtypes = [vp, C.POINTER(C.c_uint32), C.POINTER(C.POINTER(C.c_int32)),
                                        C.POINTER(C.c_uint64), C.POINTER(C.POINTER(C.c_uint32))]
+    L.fsig_read_graph_file_threads.argtypes = [C.c_char_p, C.c_int, C.c_uint64, C.POINTER(vp)]
     L.fsig_free_graph_file.argtypes = [vp]
     L.fsig_free_graph_file.restype = None
     L.fsig_match_embeddings.argtypes = [vp, C.POINTER(_Query), C.c_int, C.c_uint64, _SINK, vp, C.POINTER(_Result)]
     L.fsig_write_embeddings.argtypes = [vp, C.POINTER(_Query), C.c_int, C.c_char_p, C.POINTER(_Result)]
     for name in ("fsig_mpnn_set_params", "fsig_mpnn_get_params", "fsig_mpnn_features", "fsig_mpnn_forward",
-                 "fsig_mpnn_train_step", "fsig_read_graph_file", "fsig_graph_file_data", "fsig_match_embeddings",
+                 "fsig_mpnn_train_step", "fsig_read_graph_file", "fsig_read_graph_file_threads", "fsig_graph_file_data", "fsig_match_embeddings",
                  "fsig_write_embeddings", "fsig_filter_noalloc", "fsig_last_stats", "fsig_plan_order", "fsig_create", "fsig_destroy", "fsig_load_graph", "fsig_load_graph_file", "fsig_graph_info",
                  "fsig_match", "fsig_match_batch", "fsig_build_csr", "fsig_build_signature", "fsig_filter"):
         getattr(L, name).restype = C.c_int
@@ -237,6 +238,26 @@ class Result:
     ms_filter: float = 0.0
     ms_join: float = 0.0
     work: int = 0
+
+
+def read_graph_native(path, is_labeled: bool = True, parallel_min_bytes: int = 0) -> Graph:
+    """The C++ reader (fsig_read_graph_file_threads): labels (-1 for ids
+    without a v record) and the edge list in file order, duplicates kept.
+    Needs no GPU."""
+    L = engine_library()
+    h = C.c_void_p()
+    rc = L.fsig_read_graph_file_threads(str(path).encode(), 1 if is_labeled else 0, parallel_min_bytes, C.byref(h))
+    if rc:
+        raise FsigError(rc, f"cannot read {path}: {L.fsig_last_error(None).decode()}")
+    try:
+        V, E = C.c_uint32(), C.c_uint64()
+        lab, edg = C.POINTER(C.c_int32)(), C.POINTER(C.c_uint32)()
+        L.fsig_graph_file_data(h, C.byref(V), C.byref(lab), C.byref(E), C.byref(edg))
+        labels = np.ctypeslib.as_array(lab, shape=(V.value,)).copy() if V.value else np.zeros(0, np.int32)
+        edges = (np.ctypeslib.as_array(edg, shape=(2 * E.value,)).copy() if E.value else np.zeros(0, np.uint32))
+    finally:
+        L.fsig_free_graph_file(h)
+    return Graph(labels, edges.reshape(-1, 2))
 
 
 def read_graph(path, is_labeled: bool = True) -> Graph:

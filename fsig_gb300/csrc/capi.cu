@@ -238,13 +238,17 @@ int fsig_match(fsig_engine* h, const fsig_query* q, int algo, fsig_result* out) 
 }
 
 int fsig_read_graph_file(const char* path, int is_labeled, fsig_graph_file** out) {
+  return fsig_read_graph_file_threads(path, is_labeled, 0, out);
+}
+
+int fsig_read_graph_file_threads(const char* path, int is_labeled, uint64_t parallel_min_bytes, fsig_graph_file** out) {
   fsig::clear_thread_error();
   if (!path || !out) return FSIG_EINVAL;
   *out = nullptr;
   auto* f = new (std::nothrow) fsig_graph_file();
   if (!f) return FSIG_EINVAL;
   std::string err;
-  if (fsig::read_tve(path, is_labeled, f->g, err) != 0) {
+  if (fsig::read_tve(path, is_labeled, f->g, err, parallel_min_bytes) != 0) {
     delete f;
     fsig::fail(FSIG_EIO, err);
     return FSIG_EIO;

@@ -12,6 +12,8 @@ struct TveGraph {
   std::vector<uint32_t> edges;   // pairs, file order
 };
 
-int read_tve(const char* path, int is_labeled, TveGraph& g, std::string& err);
+// parallel_from: files of at least this many bytes are parsed with one thread
+// per core when every line is a plain record (0: 64 MiB).
+int read_tve(const char* path, int is_labeled, TveGraph& g, std::string& err, uint64_t parallel_from = 0);
 
 }  // namespace fsig

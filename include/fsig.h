@@ -125,6 +125,10 @@ int fsig_graph_info(const fsig_engine* e, uint32_t* num_vertices, uint64_t* num_
  *      edges[2 * num_edges] (file order, duplicates kept). ---- */
 typedef struct fsig_graph_file fsig_graph_file;
 int fsig_read_graph_file(const char* path, int is_labeled, fsig_graph_file** out);
+/* The same, parsing with one thread per core from parallel_min_bytes of file
+ * size on (0: 64 MiB) when every line is blank or one plain v/e record; the
+ * result is always the sequential reading's. */
+int fsig_read_graph_file_threads(const char* path, int is_labeled, uint64_t parallel_min_bytes, fsig_graph_file** out);
 int fsig_graph_file_data(const fsig_graph_file* f, uint32_t* num_vertices, const int32_t** labels,
                          uint64_t* num_edges, const uint32_t** edges);
 void fsig_free_graph_file(fsig_graph_file* f);
