@@ -270,7 +270,7 @@ def training_workloads():
     network is trained on: the 320k-vertex Chung-Lu graph (exponent 2.1,
     seed 2, 16 Zipf labels; the graph of the 8-vertex and the batched-serving
     workloads) with 8-vertex and 4-32-vertex dense and sparse random-walk
-    queries on labels >= 4.  Query seeds start at 70,000,000, apart from the
+    queries and 12-32-vertex dense ones, all on labels >= 4.  Query seeds start at 70,000,000, apart from the
     ones the benchmark draws.  The unlabeled 2^20-vertex R-MAT graph is not
     logged: none of 64 of its 5-vertex queries examines fewer than 2^26 driver
     entries, and every logged alternative order would cost as much again."""
@@ -284,7 +284,8 @@ def training_workloads():
     mixed = [(int(n), QUERY_DENSE if i % 2 else QUERY_SPARSE, 70_000_000 + i, 4)
              for i, n in enumerate(rng.integers(4, 33, 3000))]
     eight = [(8, QUERY_DENSE if i % 2 else QUERY_SPARSE, 71_000_000 + i, 4) for i in range(600)]
-    return [("chung-lu 320k", chung_lu, mixed + eight, 1 << 25)]
+    dense = [(int(n), QUERY_DENSE, 73_000_000 + i, 4) for i, n in enumerate(rng.integers(12, 33, 3000))]
+    return [("chung-lu 320k", chung_lu, mixed + eight + dense, 1 << 25)]
 
 
 def main(argv=None):
