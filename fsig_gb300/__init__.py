@@ -133,13 +133,15 @@ def engine_library() -> C.CDLL:
     L.fsig_read_graph_file.argtypes = [C.c_char_p, C.c_int, C.POINTER(vp)]
     L.fsig_graph_file_data.argtypes = [vp, C.POINTER(C.c_uint32), C.POINTER(C.POINTER(C.c_int32)),
                                        C.POINTER(C.c_uint64), C.POINTER(C.POINTER(C.c_uint32))]
+    L.fsig_save_graph_cache.argtypes = [vp, C.c_char_p]
+    L.fsig_load_graph_cache.argtypes = [vp, C.c_char_p]
     L.fsig_read_graph_file_threads.argtypes = [C.c_char_p, C.c_int, C.c_uint64, C.POINTER(vp)]
     L.fsig_free_graph_file.argtypes = [vp]
     L.fsig_free_graph_file.restype = None
     L.fsig_match_embeddings.argtypes = [vp, C.POINTER(_Query), C.c_int, C.c_uint64, _SINK, vp, C.POINTER(_Result)]
     L.fsig_write_embeddings.argtypes = [vp, C.POINTER(_Query), C.c_int, C.c_char_p, C.POINTER(_Result)]
     for name in ("fsig_mpnn_set_params", "fsig_mpnn_get_params", "fsig_mpnn_features", "fsig_mpnn_forward",
-                 "fsig_mpnn_train_step", "fsig_read_graph_file", "fsig_read_graph_file_threads", "fsig_graph_file_data", "fsig_match_embeddings",
+                 "fsig_mpnn_train_step", "fsig_read_graph_file", "fsig_read_graph_file_threads", "fsig_save_graph_cache", "fsig_load_graph_cache", "fsig_graph_file_data", "fsig_match_embeddings",
                  "fsig_write_embeddings", "fsig_filter_noalloc", "fsig_last_stats", "fsig_plan_order", "fsig_create", "fsig_destroy", "fsig_load_graph", "fsig_load_graph_file", "fsig_graph_info",
                  "fsig_match", "fsig_match_batch", "fsig_build_csr", "fsig_build_signature", "fsig_filter"):
         getattr(L, name).restype = C.c_int
@@ -423,6 +425,12 @@ class Engine:
     def load_graph_file(self, path, is_labeled: bool = True) -> None:
         self._check(self._L.fsig_load_graph_file(self._h, str(path).encode(), 1 if is_labeled else 0),
                     "load_graph_file")
+
+    def save_graph_cache(self, path) -> None:
+        self._check(self._L.fsig_save_graph_cache(self._h, str(path).encode()), "save_graph_cache")
+
+    def load_graph_cache(self, path) -> None:
+        self._check(self._L.fsig_load_graph_cache(self._h, str(path).encode()), "load_graph_cache")
 
     def graph_info(self) -> dict:
         V, nadj, L, md = C.c_uint32(), C.c_uint64(), C.c_int32(), C.c_uint32()

@@ -206,6 +206,20 @@ int fsig_load_graph_file(fsig_engine* h, const char* path, int is_labeled) {
                                             g.edges.data()));
 }
 
+int fsig_save_graph_cache(fsig_engine* h, const char* path) {
+  int rc = select(h);
+  if (rc) return finish(h, rc);
+  if (!path) return finish(h, fsig::fail(FSIG_EINVAL, "no path"));
+  return finish(h, fsig::save_graph_cache(h->e, path));
+}
+
+int fsig_load_graph_cache(fsig_engine* h, const char* path) {
+  int rc = select(h);
+  if (rc) return finish(h, rc);
+  if (!path) return finish(h, fsig::fail(FSIG_EINVAL, "no path"));
+  return finish(h, fsig::load_graph_cache(h->e, path));
+}
+
 int fsig_graph_info(const fsig_engine* h, uint32_t* V, uint64_t* nadj, int32_t* L, uint32_t* maxdeg) {
   if (!h) return FSIG_EINVAL;
   if (!h->e.has_graph) return FSIG_ENOGRAPH;

@@ -61,6 +61,8 @@ struct Engine {
 
 // graph_store.cu
 int build_device_graph(Engine& e, uint32_t V, const int32_t* labels, uint64_t E, const uint32_t* edges);
+int save_graph_cache(Engine& e, const char* path);
+int load_graph_cache(Engine& e, const char* path);
 int build_reference_csr(Engine& e, uint32_t V, uint64_t E, const uint32_t* edges, uint32_t* offsets,
                         uint32_t* adj);
 int build_reference_signature(Engine& e, uint32_t V, const int32_t* labels, const uint32_t* offsets,

@@ -3,6 +3,8 @@
 // tables.  Replaces the host loops of graph_format_transformer.cc:12-37 and
 // :217-281 and the per-buffer copies of match/MMatch.cu:14-32.
 #include <algorithm>
+#include <cstdio>
+#include <cstring>
 
 #include "engine.h"
 #include "scan.cuh"
@@ -474,6 +476,115 @@ int build_device_graph(Engine& e, uint32_t V, const int32_t* h_labels, uint64_t 
     FSIG_CUDA_TRY(cudaStreamSynchronize(s));
     e.arena.release(mm);
   }
+  g.arena_mark = e.arena.mark();
+  e.g = g;
+  e.has_graph = true;
+  return FSIG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Binary cache of the resident graph store: a header, then the device arrays
+// as they are (renumbered ids, CSR, caller ids, label segments, signatures),
+// so that a later load is a file read and host-to-device copies, with no
+// parsing, sorting or segment building.
+// ---------------------------------------------------------------------------
+namespace {
+constexpr char kCacheMagic[8] = {'F', 'S', 'I', 'G', 'G', 'S', '0', '1'};
+
+struct CacheHeader {
+  char magic[8];
+  uint32_t V;
+  int32_t L;
+  uint64_t nadj;
+  uint32_t max_deg;
+  uint32_t pad;
+};
+
+struct CacheArray {
+  void* dev;
+  uint64_t bytes;
+};
+
+std::vector<CacheArray> cache_arrays(const DeviceGraph& g) {
+  const uint64_t V = g.V, L1 = uint64_t(g.L) + 1;
+  return {{g.label, 4 * V},           {g.old_of_new, 4 * V},     {g.new_of_old, 4 * V},
+          {g.base, 4 * L1},           {g.off, 4 * (V + 1)},      {g.adj, 4 * g.nadj},
+          {g.adj_old, 4 * g.nadj},    {g.lseg, 4 * V * L1},      {g.sig, 64 * V}};
+}
+}  // namespace
+
+int save_graph_cache(Engine& e, const char* path) {
+  if (!e.has_graph) return fail(FSIG_ENOGRAPH, "no data graph loaded");
+  const DeviceGraph& g = e.g;
+  FILE* f = std::fopen(path, "wb");
+  if (!f) return fail(FSIG_EIO, std::string("cannot open ") + path);
+  CacheHeader h{};
+  std::memcpy(h.magic, kCacheMagic, 8);
+  h.V = g.V;
+  h.L = g.L;
+  h.nadj = g.nadj;
+  h.max_deg = g.max_deg;
+  bool ok = std::fwrite(&h, sizeof h, 1, f) == 1;
+  std::vector<char> buf;
+  for (const CacheArray& a : cache_arrays(g)) {
+    if (!ok) break;
+    buf.resize(a.bytes);
+    if (a.bytes) {
+      const cudaError_t err = cudaMemcpy(buf.data(), a.dev, a.bytes, cudaMemcpyDeviceToHost);
+      if (err != cudaSuccess) {
+        std::fclose(f);
+        return fail_cuda(err, "cudaMemcpy", __FILE__, __LINE__);
+      }
+      ok = std::fwrite(buf.data(), 1, a.bytes, f) == a.bytes;
+    }
+  }
+  if (std::fclose(f) != 0) ok = false;
+  return ok ? FSIG_OK : fail(FSIG_EIO, std::string("cannot write ") + path);
+}
+
+int load_graph_cache(Engine& e, const char* path) {
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return fail(FSIG_EIO, std::string("cannot open ") + path);
+  CacheHeader h{};
+  if (std::fread(&h, sizeof h, 1, f) != 1 || std::memcmp(h.magic, kCacheMagic, 8) != 0 || h.V == 0 || h.L < 1) {
+    std::fclose(f);
+    return fail(FSIG_EIO, std::string(path) + " is not a graph cache of this engine");
+  }
+  e.arena.release(0);
+  e.has_graph = false;
+  DeviceGraph g;
+  g.V = h.V;
+  g.L = h.L;
+  g.nadj = h.nadj;
+  g.max_deg = h.max_deg;
+  const uint64_t V = g.V, L1 = uint64_t(g.L) + 1;
+  g.label = e.arena.take<int32_t>(V);
+  g.old_of_new = e.arena.take<uint32_t>(V);
+  g.new_of_old = e.arena.take<uint32_t>(V);
+  g.off = e.arena.take<uint32_t>(V + 1);
+  g.adj = e.arena.take<uint32_t>(std::max<uint64_t>(g.nadj, 1));
+  g.base = e.arena.take<uint32_t>(L1);
+  g.lseg = e.arena.take<uint32_t>(V * L1);
+  g.sig = e.arena.take<uint4>(V * 4);
+  g.adj_old = e.arena.take<uint32_t>(std::max<uint64_t>(g.nadj, 1));
+  if (!g.label || !g.old_of_new || !g.new_of_old || !g.off || !g.adj || !g.base || !g.lseg || !g.sig || !g.adj_old) {
+    std::fclose(f);
+    e.arena.release(0);
+    return fail(FSIG_EADMISSION, "graph does not fit the device arena");
+  }
+  std::vector<char> buf;
+  for (const CacheArray& a : cache_arrays(g)) {
+    buf.resize(a.bytes);
+    if (a.bytes && std::fread(buf.data(), 1, a.bytes, f) != a.bytes) {
+      std::fclose(f);
+      e.arena.release(0);
+      return fail(FSIG_EIO, std::string(path) + " is truncated");
+    }
+    if (a.bytes) FSIG_CUDA_TRY(cudaMemcpy(a.dev, buf.data(), a.bytes, cudaMemcpyHostToDevice));
+  }
+  std::fclose(f);
+  g.h_base.resize(L1);
+  FSIG_CUDA_TRY(cudaMemcpy(g.h_base.data(), g.base, 4 * L1, cudaMemcpyDeviceToHost));
   g.arena_mark = e.arena.mark();
   e.g = g;
   e.has_graph = true;

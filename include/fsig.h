@@ -119,6 +119,13 @@ int fsig_load_graph_file(fsig_engine* e, const char* path, int is_labeled);
 int fsig_graph_info(const fsig_engine* e, uint32_t* num_vertices, uint64_t* num_adj,
                     int32_t* num_labels, uint32_t* max_degree);
 
+/* Binary cache of the resident graph store (the device arrays as built: the
+ * renumbered CSR, caller ids, label segments and signatures), in place of the
+ * reference's commented-out binary PCSR dump (graph_format_transformer.cc:47-74,
+ * 197-213): a load is a file read and copies, no parsing or building. */
+int fsig_save_graph_cache(fsig_engine* e, const char* path);
+int fsig_load_graph_cache(fsig_engine* e, const char* path);
+
 /* ---- host reader; replaces UndirectedSurveyPlainReader::read (IO/graph_reader.cc:12-55)
  *      for callers that want the parsed graph itself (query files, the CLI).
  *      The handle owns labels[num_vertices] (-1 for ids without a v record) and

@@ -306,3 +306,25 @@ def test_cuda_graph_batches_match_stream_batches(engine, config2_small, algo):
             r = engine.match_batch(part, algo=algo, use_graph=True, **kw)
             assert engine.last_stats()["graph"] == 1
             assert [(x.count, x.hash, x.level_counts, x.order) for x in r] == want[: len(part)]
+
+
+def test_graph_cache_round_trip(engine, golden, tmp_path):
+    """A graph store saved to the binary cache and loaded into another engine
+    matches every golden query exactly as the built one does."""
+    rec = golden["graphs"]["cl_zipf16"]
+    engine.load_graph(F.read_graph(GOLDEN / rec["file"], True))
+    qs = golden_queries(golden)
+    want = [(r.count, r.hash, r.order) for r in engine.match_batch(qs, algo=F.ALGO_FUSED)]
+    info = engine.graph_info()
+    path = tmp_path / "cl_zipf16.fsigcache"
+    engine.save_graph_cache(path)
+    with F.Engine(0, arena_bytes=1 << 30) as other:
+        other.load_graph_cache(path)
+        assert other.graph_info() == info
+        got = [(r.count, r.hash, r.order) for r in other.match_batch(qs, algo=F.ALGO_FUSED)]
+        assert got == want
+        assert [(r.count, r.hash) for r in (other.match(q, F.ALGO_FSIG) for q in qs[:4])] == [w[:2] for w in want[:4]]
+    (tmp_path / "bad.fsigcache").write_bytes(b"not a cache")
+    with pytest.raises(F.FsigError) as ei:
+        engine.load_graph_cache(tmp_path / "bad.fsigcache")
+    assert ei.value.status == F.EIO
