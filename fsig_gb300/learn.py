@@ -153,11 +153,13 @@ class QueryLog:
     level_counts: list      # per alternative
     aborted: int            # alternatives stopped by the limit
 
+    margin = 0.98  # an alternative replaces the heuristic order below this fraction of its work
+
     @property
     def best(self):
         """The cheapest order found; the heuristic order unless an alternative
-        examined at least 2% fewer entries."""
-        if self.works and min(self.works) < 0.98 * self.heuristic_work:
+        examined fewer than `margin` times its entries."""
+        if self.works and min(self.works) < self.margin * self.heuristic_work:
             i = int(np.argmin(self.works))
             return self.orders[i], self.works[i]
         return self.heuristic_order, self.heuristic_work
@@ -204,8 +206,13 @@ def collect_logs(engine: Engine, queries: Sequence[Query], algo: int = ALGO_FUSE
     return logs
 
 
-def training_set(engine: Engine, logs: Sequence[QueryLog], algo: int = ALGO_FUSED):
-    """(node offsets, features, neighbour masks, targets) for the logs."""
+def training_set(engine: Engine, logs: Sequence[QueryLog], algo: int = ALGO_FUSED, margin: float | None = None):
+    """(node offsets, features, neighbour masks, targets) for the logs; with
+    margin, an alternative must be cheaper than margin x the heuristic's work
+    to become the target."""
+    if margin is not None:
+        for lg in logs:
+            lg.margin = margin
     qs = [lg.query for lg in logs]
     feat = engine.mpnn_features(qs, [lg.candidates for lg in logs], algo)
     goff = np.zeros(len(qs) + 1, np.uint32)
@@ -301,6 +308,8 @@ def main(argv=None):
     ap.add_argument("--work-limit", type=int, default=0,
                     help="drop queries whose heuristic run examines more (default: per workload)")
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--margin", type=float, default=0.98,
+                    help="an alternative order becomes the target below this fraction of the heuristic's work")
     ap.add_argument("--device", type=int, default=0)
     args = ap.parse_args(argv)
     logs = []
@@ -317,7 +326,7 @@ def main(argv=None):
             gain = sum(x.heuristic_work for x in lg) / max(sum(x.best[1] for x in lg), 1)
             print(f"[learn] {name}: {len(lg)} queries logged, best/heuristic total work 1/{gain:.3f}, "
                   f"{time.time() - t0:.1f}s", flush=True)
-            logs.append((lg, training_set(e, lg)))
+            logs.append((lg, training_set(e, lg, margin=args.margin)))
         goff = np.zeros(1, np.uint32)
         feats, nbrs, tgts = [], [], []
         for _, (o, f, nb, t) in logs:
