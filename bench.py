@@ -60,11 +60,10 @@ PEAKS = ROOT / "MEASURED_PEAKS.json"
 FALLBACK_HBM_GBS = 6800.0
 
 # DRAM bytes per enumeration launch from an ncu capture; None until measured.
-# DRAM bytes (read + write) of one enumerate_kernel launch on the heavy
-# config-5 batch, from an ncu capture (profiles/enumerate_kernel_c5.md); the
-# launch examined 5.36e8 driver windows and requested ~0.66 TB, nearly all
-# served by L2.
-ENUM_TRAFFIC_BYTES_PER_LAUNCH = 438_840_000
+# DRAM bytes (read + write) of one enumerate_kernel launch on a heavy
+# config-5 batch (about 5.4e8 driver windows), from an ncu capture
+# (profiles/enumerate_kernel_c5.md); its loads are served from L2 at 98.9%.
+ENUM_TRAFFIC_BYTES_PER_LAUNCH = 286_300_000
 
 
 def log(*a):
@@ -482,7 +481,7 @@ def run_ours(args, dist):
                      "peak_source": "measured" if PEAKS.exists() else "fallback",
                      "traffic": ENUM_TRAFFIC_BYTES_PER_LAUNCH,
                      "traffic_note": "DRAM bytes of one heavy config-5 batch launch (ncu); requested bytes are "
-                                     "served from L2 at 98.6% hit: the kernel is issue-bound, not HBM-bound",
+                                     "served from L2 at 98.9% hit: the kernel is issue-bound, not HBM-bound",
                      "achieved_basis": "bytes requested by the kernel's global loads / kernel time, "
                                        + roof_basis},
         "clocks": clocks,
