@@ -479,9 +479,10 @@ def run_ours(args, dist):
         "roofline": {"bound": "hbm", "kernel": "enumerate_kernel", "achieved": round(achieved, 1),
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
                      "peak_source": "measured" if PEAKS.exists() else "fallback",
-                     "traffic": ENUM_TRAFFIC_BYTES_PER_LAUNCH,
-                     "traffic_note": "DRAM bytes of one heavy config-5 batch launch (ncu); requested bytes are "
-                                     "served from L2 at 98.9% hit: the kernel is issue-bound, not HBM-bound",
+                     "traffic": ENUM_TRAFFIC_BYTES_PER_LAUNCH if args.workload == "c5" else None,
+                     "traffic_note": ("DRAM bytes of one heavy config-5 batch launch (ncu); requested bytes are "
+                                      "served from L2 at 98.9% hit: the kernel is issue-bound, not HBM-bound")
+                                     if args.workload == "c5" else "no ncu capture of this workload",
                      "achieved_basis": "bytes requested by the kernel's global loads / kernel time, "
                                        + roof_basis},
         "clocks": clocks,
