@@ -55,7 +55,7 @@ class _Result(C.Structure):
 class _BatchOpts(C.Structure):
     _fields_ = [("algo", C.c_int), ("order_source", C.c_int), ("refine_iters", C.c_int), ("use_graph", C.c_int),
                 ("chunk", C.c_uint32), ("split_len", C.c_uint32), ("split_cycles", C.c_uint64),
-                ("max_work", C.c_uint64), ("warps_per_block", C.c_uint32), ("reserved", C.c_uint32)]
+                ("max_work", C.c_uint64), ("warps_per_block", C.c_uint32), ("learned_window", C.c_uint32)]
 
 
 class _Stats(C.Structure):
@@ -448,14 +448,15 @@ class Engine:
 
     def match_batch(self, qs: Sequence[Query], algo: int = ALGO_FUSED, order_source: int = ORDER_HEURISTIC,
                     refine_iters: int = -1, chunk: int = 0, use_graph: bool = False, split_len: int = 0,
-                    split_cycles: int = 0, max_work: int = 0, warps_per_block: int = 0) -> list:
+                    split_cycles: int = 0, max_work: int = 0, warps_per_block: int = 0,
+                    learned_window: int = 0) -> list:
         keep = []
         arr = (_Query * max(len(qs), 1))()
         for i, q in enumerate(qs):
             arr[i] = _as_cquery(q, keep)
         res = (_Result * max(len(qs), 1))()
         opts = _BatchOpts(algo, order_source, refine_iters, 1 if use_graph else 0, chunk, split_len, split_cycles,
-                          max_work, warps_per_block, 0)
+                          max_work, warps_per_block, learned_window)
         self._check(self._L.fsig_match_batch(self._h, len(qs), arr, C.byref(opts), res), "match_batch")
         return [_result(res[i]) for i in range(len(qs))]
 

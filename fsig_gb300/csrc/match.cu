@@ -561,6 +561,23 @@ float elapsed(cudaEvent_t a, cudaEvent_t b) {
   return ms;
 }
 
+// Keeps the network's order near the heuristic one: the score of the vertex
+// at heuristic position i is clamped to positions [i - window, i + window]
+// (scores are positions / (n - 1)); thread per query.
+__global__ void order_window_kernel(const uint32_t* __restrict__ qoff, uint32_t Q,
+                                    const uint32_t* __restrict__ horders, uint32_t window, float* scores) {
+  for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < Q; q += gridDim.x * blockDim.x) {
+    const uint32_t g0 = qoff[q], n = qoff[q + 1] - g0;
+    if (n < 2) continue;
+    const float scale = float(n - 1);
+    for (uint32_t i = 0; i < n; i++) {
+      const uint32_t u = horders[uint64_t(q) * kMaxQ + i];
+      const float lo = float(i > window ? i - window : 0u), hi = float(i + window);
+      scores[g0 + u] = fminf(fmaxf(scores[g0 + u] * scale, lo), hi) / scale;
+    }
+  }
+}
+
 // In a learned-order batch, queries that carry their own order keep it: their
 // scores become the positions of that order (thread per query).
 __global__ void given_scores_kernel(const uint32_t* __restrict__ qoff, uint32_t Q,
@@ -888,6 +905,12 @@ int run_batch(Engine& e, const std::vector<HostQuery>& qs, const BatchOptions& o
       rc = mpnn_forward_device(e, Q, d_qoff, d_feat, d_nbr, d_lscores);
       if (rc) return rc;
       launches += 3;
+      if (opt.learned_window < kMaxQ) {
+        order_window_kernel<<<std::max<uint32_t>(1, (Q + 127) / 128), 128, 0, s>>>(d_qoff, Q, d_orders,
+                                                                                 opt.learned_window, d_lscores);
+        FSIG_CUDA_TRY(cudaGetLastError());
+        launches++;
+      }
       if (any_given) {
         uint32_t* d_has_given = stage_upload(e, st, has_given, rc);
         if (rc) return rc;

@@ -87,6 +87,7 @@ struct BatchOptions {
   uint32_t warps_per_block = 8;
   const float* scores = nullptr;  // host scores per query vertex (kOrderScores), batch order
   bool learned = false;           // score with the loaded order network (kOrderScores)
+  uint32_t learned_window = 32;   // positions a vertex may move from the heuristic order (32: any)
   // Single-query batches only: write up to emit_cap embeddings to
   // BatchOutput::rows, and enumerate only pass-0 tasks [task_begin, task_end).
   uint64_t emit_cap = 0;

@@ -96,7 +96,8 @@ typedef struct {
                             scheduling: it is set iff the query's total work
                             under its order exceeds the limit (0: no limit)     */
   uint32_t warps_per_block; /* enumeration block size in warps, 1..8 (0: default 8) */
-  uint32_t reserved;
+  uint32_t learned_window;  /* FSIG_ORDER_LEARNED: positions a vertex may move away
+                               from the heuristic order (0: any)                 */
 } fsig_batch_opts;
 
 /* ---- engine lifetime; replaces GPUSubgraphMatcher::init_GPU (match/subgraph_match.h:51-80)
