@@ -198,7 +198,9 @@ __global__ void __launch_bounds__(256, 4) enumerate_kernel(EnumArgs A) {
       bytes += 8;
     }
     const bool empty = __ballot_sync(kFull, len == 0) != 0;
-    const uint32_t j = warp_argmin(float(len), len == kInvalid ? 0xffffu : lane) & 31u;
+    // shortest segment, lowest lane on ties: one warp reduction of (length, lane)
+    const uint32_t key = len == kInvalid ? 0xffffffffu : (min(len, (1u << 27) - 1u) << 5) | lane;
+    const uint32_t j = __reduce_min_sync(kFull, key) & 31u;
     const uint32_t dlo = __shfl_sync(kFull, lo, j), dhi = __shfl_sync(kFull, hi, j);
     if (lane == lv) {
       if (lo_set != kInvalid) {
