@@ -1,6 +1,7 @@
 """Unlabeled counting (the config-3 case, graph_type = 0) at reduced scale:
-an R-MAT graph (seed 3) with 2^14 vertices and 2^18 edges, no labels, and the
-five 5-vertex patterns -- K4 plus a pendant vertex, the 5-cycle, the house and
+R-MAT graphs (seed 3) with 2^10 vertices and 2^13 edges (up to 7e8
+embeddings per pattern) and with 2^8 vertices and 2^11 edges (the oracle
+checks every pattern there), no labels, and the five 5-vertex patterns -- K4 plus a pendant vertex, the 5-cycle, the house and
 two seeded random connected graphs.  Skewed degree lists stress the segment
 searches.  Pins: the K4+pendant identity (its count is the sum over ordered
 K4 embeddings of deg(image of the attach vertex) - 3, with the K4 embeddings
@@ -48,7 +49,14 @@ PATTERNS = {
 
 @pytest.fixture(scope="module")
 def rmat():
-    g = F.gen_rmat(1 << 14, 1 << 18, 0.57, 0.19, 0.19, seed=3)
+    g = F.gen_rmat(1 << 10, 1 << 13, 0.57, 0.19, 0.19, seed=3)
+    off, adj = g.csr()
+    return g, off, adj
+
+
+@pytest.fixture(scope="module")
+def tiny():
+    g = F.gen_rmat(1 << 8, 1 << 11, 0.57, 0.19, 0.19, seed=3)
     off, adj = g.csr()
     return g, off, adj
 
@@ -74,6 +82,14 @@ def test_algorithms_and_batch_agree(engine, rmat, name):
     res += engine.match_batch([q] * 3, algo=F.ALGO_FUSED, use_graph=True)
     assert len({(r.count, r.hash) for r in res}) == 1
     assert res[0].count > 0
-    if res[0].count <= 20_000_000:
-        c, h, _ = O.match(g.labels, off, adj, q.labels, q.edges)
-        assert (res[0].count, res[0].hash) == (c, h)
+
+
+@pytest.mark.parametrize("name", sorted(PATTERNS))
+def test_patterns_match_oracle(engine, tiny, name):
+    g, off, adj = tiny
+    engine.load_graph(g)
+    q = pattern(PATTERNS[name])
+    c, h, _ = O.match(g.labels, off, adj, q.labels, q.edges)
+    for a in (F.ALGO_FSIG, F.ALGO_GSI, F.ALGO_FUSED):
+        r = engine.match(q, a)
+        assert (r.count, r.hash) == (c, h)
