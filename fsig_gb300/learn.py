@@ -4,7 +4,7 @@ forward and backward kernels (``fsig_mpnn_train_step``).
 
 The reference has no counterpart: it orders by heuristics only
 (match/GSI.cu:105-149, match/MMatch.cu:1575-1641).  Here the heuristic order
-stays the fallback and the judge of cost:
+stays the fallback and the measure of cost:
 
 * a log records, per query, the heuristic order and a set of alternative
   connected orders, each with the driver entries its enumeration examined
