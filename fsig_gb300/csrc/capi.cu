@@ -378,7 +378,7 @@ int fsig_match_batch(fsig_engine* h, uint32_t nq, const fsig_query* qs, const fs
   o.use_graph = bo.use_graph != 0;
   if (bo.learned_window) o.learned_window = bo.learned_window;
   if (bo.warps_per_block) {
-    if (bo.warps_per_block > 8) return finish(h, fsig::fail(FSIG_EINVAL, "warps_per_block must be 1..8"));
+    if (bo.warps_per_block > fsig::kEnumWarps) return finish(h, fsig::fail(FSIG_EINVAL, "warps_per_block too large"));
     o.warps_per_block = bo.warps_per_block;
   }
   if (bo.chunk) o.chunk = bo.chunk;

@@ -46,7 +46,7 @@ struct Engine {
   void* pinned = nullptr;
   uint64_t pinned_bytes = 0;
   // enumeration kernel: resident blocks per SM (0 until first queried)
-  int enum_per_sm = 0;
+  int enum_per_sm[9] = {0};  // resident blocks per SM at 1..8 warps per block (0 until queried)
   // timing events
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   cudaEvent_t ev_enum[2] = {nullptr, nullptr};

@@ -125,7 +125,7 @@ __device__ __forceinline__ uint32_t warp_lower_bound(const uint32_t* __restrict_
   return lo + __popc(__ballot_sync(kFull, in && v < key));
 }
 
-__global__ void __launch_bounds__(256, 4) enumerate_kernel(EnumArgs A) {
+__global__ void __launch_bounds__(kEnumWarps * 32, kEnumMinBlocks) enumerate_kernel(EnumArgs A) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   WarpSmem& ws = reinterpret_cast<WarpSmem*>(smem_raw)[threadIdx.x >> 5];
   const uint32_t lane = threadIdx.x & 31;

@@ -613,12 +613,15 @@ struct EnumRun {
 
 // One-time kernel attributes and occupancy (host calls, kept out of captures).
 int enum_configure(Engine& e) {
-  if (e.enum_per_sm) return FSIG_OK;
+  if (e.enum_per_sm[kEnumWarps]) return FSIG_OK;
   FSIG_CUDA_TRY(cudaFuncSetAttribute(enumerate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     int(sizeof(WarpSmem) * 8)));
-  int per = 0;
-  FSIG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, enumerate_kernel, 8 * 32, sizeof(WarpSmem) * 8));
-  e.enum_per_sm = std::max(per, 1);
+                                     int(sizeof(WarpSmem) * kEnumWarps)));
+  for (uint32_t w = 1; w <= kEnumWarps; w++) {
+    int per = 0;
+    FSIG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, enumerate_kernel, int(w * 32),
+                                                                sizeof(WarpSmem) * w));
+    e.enum_per_sm[w] = std::max(per, 1);
+  }
   return FSIG_OK;
 }
 
@@ -639,8 +642,8 @@ int enum_prepare(Engine& e, const BatchOptions& opt, const GraphView& gv, const 
   FSIG_CUDA_TRY(cudaMemsetAsync(rb, 0, sizeof(uint32_t) * kOverflowCap, s));
   FSIG_CUDA_TRY(cudaMemsetAsync(R.d_ev, 0, 64, s));
   FSIG_CUDA_TRY(cudaMemsetAsync(d_misc + 1, 0, sizeof(unsigned long long), s));
-  const uint32_t wpb = std::max<uint32_t>(1, std::min<uint32_t>(opt.warps_per_block, 8));
-  const int per_sm = wpb == 8 ? e.enum_per_sm : std::max(1, e.enum_per_sm * 8 / int(wpb));
+  const uint32_t wpb = std::max<uint32_t>(1, std::min<uint32_t>(opt.warps_per_block, kEnumWarps));
+  const int per_sm = e.enum_per_sm[wpb];
   R.smem = sizeof(WarpSmem) * wpb;
   R.grid = uint32_t(e.num_sms * per_sm);
   R.block = wpb * 32;

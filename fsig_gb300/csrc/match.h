@@ -76,6 +76,11 @@ struct QueryResult {
   unsigned int pad;
 };
 
+// Enumeration launch shape: at most kEnumWarps warps per block, compiled for
+// kEnumMinBlocks resident blocks per SM (which caps registers per thread).
+constexpr uint32_t kEnumWarps = 8;
+constexpr uint32_t kEnumMinBlocks = 4;
+
 struct BatchOptions {
   uint32_t filter_mode = kFilterDegree | kFilterSignature;
   int refine_iters = 0;
@@ -84,7 +89,7 @@ struct BatchOptions {
   uint32_t split = 256;      // driver entries per task range
   long long budget_cycles = 4000;     // cycles on a task before it may be split for idle warps
   unsigned long long max_work = 0;  // per-query limit on examined driver entries (0: none)
-  uint32_t warps_per_block = 8;
+  uint32_t warps_per_block = kEnumWarps;
   const float* scores = nullptr;  // host scores per query vertex (kOrderScores), batch order
   bool learned = false;           // score with the loaded order network (kOrderScores)
   uint32_t learned_window = 32;   // positions a vertex may move from the heuristic order (32: any)
