@@ -1,0 +1,125 @@
+"""Host-side logic of the learned order, the autotuner and the bench's
+fallback feed, against fake engines (no GPU)."""
+import numpy as np
+import pytest
+
+import fsig_gb300 as F
+from fsig_gb300 import autotune, learn
+
+
+class FakeResult:
+    def __init__(self, count, hash_, status=0, work=0, candidates=None, order=None):
+        self.count, self.hash, self.status, self.work = count, hash_, status, work
+        self.candidates = candidates or []
+        self.order = order or []
+        self.level_counts = []
+
+
+def query(n, extra=()):
+    edges = [(i, i + 1) for i in range(n - 1)] + list(extra)
+    return F.Query(np.zeros(n, np.int32), np.asarray(edges, np.uint32))
+
+
+class KnobEngine:
+    """Device time depends on the knobs; results never do (unless broken)."""
+
+    def __init__(self, broken=None):
+        self.broken = broken
+        self.ms = 0.0
+
+    def match_batch(self, qs, **kw):
+        self.ms = 10.0 + abs(kw.get("chunk", 1) - 2) + abs(kw.get("split_len", 256) - 512) / 256 \
+            + (0 if kw.get("warps_per_block", 8) == 8 else 1) + abs(kw.get("split_cycles", 4000) - 16000) / 16000
+        bad = self.broken is not None and kw.get("chunk") == self.broken
+        return [FakeResult(i + (1 if bad else 0), 7 * i) for i, _ in enumerate(qs)]
+
+    def last_stats(self):
+        return {"ms_filter": 0.0, "ms_join": self.ms}
+
+
+def test_autotune_finds_the_fastest_setting():
+    best, trials = autotune.tune(KnobEngine(), [query(3)] * 4, repeats=1)
+    assert best == {"warps_per_block": 8, "chunk": 2, "split_len": 512, "split_cycles": 16000}
+    assert trials[0][0] == autotune.DEFAULTS
+
+
+def test_autotune_rejects_a_setting_that_changes_results():
+    with pytest.raises(RuntimeError):
+        autotune.tune(KnobEngine(broken=8), [query(3)] * 4, repeats=1)
+
+
+@pytest.mark.parametrize("n", [2, 5, 9, 16])
+def test_alternative_orders_are_distinct_connected_permutations(n):
+    q = query(n, extra=[(0, n - 1)] if n > 2 else [])
+    masks = learn.adjacency_masks(q)
+    rng = np.random.default_rng(n)
+    heur = list(range(n))
+    alts = learn.alternative_orders(q, list(range(1, n + 1)), 12, rng, around=heur)
+    assert len({tuple(o) for o in alts}) == len(alts)
+    assert heur not in alts
+    for o in alts:
+        assert sorted(o) == heur and learn.is_connected_order(o, masks)
+
+
+def test_best_order_needs_the_margin():
+    lg = learn.QueryLog(query(3), [1, 1, 1], 5, 9, [0, 1, 2], 100, [[1, 0, 2], [2, 1, 0]], [99, 97], [], 0)
+    assert lg.best == ([2, 1, 0], 97)           # 97 < 0.98 x 100
+    lg.works = [99, 98.5]
+    assert lg.best == ([0, 1, 2], 100)          # neither is 2% cheaper
+    lg.works = [99, 97]
+    lg.margin = 0.9
+    assert lg.best == ([0, 1, 2], 100)          # 97 is not 10% cheaper
+
+
+def test_training_targets_are_positions_of_the_best_order():
+    class FeatEngine:
+        def mpnn_features(self, qs, cands, algo):
+            return np.zeros((sum(q.num_vertices for q in qs), 8), np.float32)
+    logs = [learn.QueryLog(query(3), [1, 1, 1], 1, 1, [0, 1, 2], 10, [[2, 1, 0]], [1], [], 0),
+            learn.QueryLog(query(2), [1, 1], 1, 1, [0, 1], 10, [], [], [], 0)]
+    goff, feat, nbr, tgt = learn.training_set(FeatEngine(), logs)
+    assert list(goff) == [0, 3, 5]
+    assert list(tgt) == [1.0, 0.5, 0.0, 0.0, 1.0]
+    assert list(nbr[:3]) == [0b010, 0b101, 0b010]
+
+
+class FeedEngine:
+    """A learned batch puts query 'x' over the limit; given orders are kept."""
+
+    def __init__(self):
+        self.calls = []
+
+    def match_batch(self, qs, **kw):
+        self.calls.append([q.order is not None for q in qs])
+        out = []
+        for q in qs:
+            tag = int(q.labels[0])
+            if tag == 99 and q.order is None:
+                out.append(FakeResult(0, 0, status=F.ELIMIT, candidates=[3, 2, 1]))
+            else:
+                out.append(FakeResult(tag, tag * 10))
+        return out
+
+    def last_stats(self):
+        return {"ms_filter": 0.0, "ms_join": 1.0, "ms_enum": 1.0, "enum_bytes": 0, "kernel_launches": 1,
+                "enum_passes": 1, "h2d_bytes": 0, "d2h_bytes": 0}
+
+
+def test_fallbacks_ride_along_in_the_next_batch(monkeypatch):
+    import bench
+    monkeypatch.setattr(F, "plan_order", lambda q, algo, cand: {"order": [2, 1, 0]})
+    eng = FeedEngine()
+    feed = bench.LearnedFeed(eng, F.ALGO_FUSED, 1 << 20, False, {})
+
+    def q(tag):
+        return F.Query(np.full(3, tag, np.int32), np.asarray([(0, 1), (1, 2)], np.uint32))
+
+    batches = [[q(1), q(99)], [q(2), q(3)]]
+    results = [None, None]
+    acc = bench.StepStats()
+    _, fb0 = feed.step(0, batches[0], acc, results)
+    _, fb1 = feed.step(1, batches[1], acc, results)
+    feed.flush(acc, results)
+    assert (fb0, fb1) == (1, 0)
+    assert eng.calls == [[False, False], [False, False, True]]  # the fallback rides in batch 1 with its order
+    assert results == [[(1, 10), (99, 990)], [(2, 20), (3, 30)]]
