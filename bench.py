@@ -288,45 +288,6 @@ class StepStats:
         self.d2h += st["d2h_bytes"]
 
 
-class LearnedFeed:
-    """Learned-order batches.  A query over the work limit (the fallback) is
-    carried into the next batch with its heuristic order attached, which a
-    learned-order batch keeps; those left after the last batch run in a batch
-    of their own at flush().  Results are written into results[step][i]."""
-
-    def __init__(self, e, algo, limit, use_graph, knobs):
-        self.e, self.algo, self.limit, self.use_graph, self.knobs = e, algo, limit, use_graph, knobs
-        self.pending = []  # (step, index, query with its heuristic order)
-
-    def _run(self, qs, acc):
-        rs = self.e.match_batch(qs, algo=self.algo, order_source=F.ORDER_LEARNED, max_work=self.limit,
-                                use_graph=self.use_graph, **self.knobs)
-        acc.add(self.e.last_stats())
-        return rs
-
-    def _settle(self, rs, results):
-        for (k, i, _), r in zip(self.pending, rs):
-            if r.status != F.OK:
-                raise RuntimeError(f"fallback query failed with status {r.status}")
-            results[k][i] = (r.count, r.hash)
-        self.pending = []
-
-    def step(self, k, b, acc, results):
-        rs = self._run(list(b) + [q for _, _, q in self.pending], acc)
-        self._settle(rs[len(b):], results)
-        rs = rs[: len(b)]
-        results[k] = [(r.count, r.hash) for r in rs]
-        for i, r in enumerate(rs):
-            if r.status == F.ELIMIT:
-                order = F.plan_order(b[i], F.ALGO_GSI, r.candidates)["order"]
-                self.pending.append((k, i, F.Query(b[i].labels, b[i].edges, order=np.asarray(order, np.uint32))))
-        return rs, sum(1 for r in rs if r.status == F.ELIMIT)
-
-    def flush(self, acc, results):
-        if self.pending:
-            self._settle(self._run([q for _, _, q in self.pending], acc), results)
-
-
 def run_ours(args, dist):
     from fsig_gb300 import learn
     dev = dist.local
@@ -351,11 +312,11 @@ def run_ours(args, dist):
             tune_note = f"coordinate descent on the last batch, {len(trials)} trials, {time.time() - t:.1f}s"
             log(f"[bench] autotuned {knobs} ({tune_note})")
 
-        feed = LearnedFeed(e, algo, limit, use_graph, knobs) if order == "learned" else None
+        feed = learn.LearnedFeed(e, algo, limit, use_graph=use_graph, **knobs) if order == "learned" else None
 
         def step(k, b, acc, results):
             if feed:
-                return feed.step(k, b, acc, results)
+                return feed.step(k, b, results, acc.add)
             rs = e.match_batch(b, algo=algo, order_source=F.ORDER_HEURISTIC, max_work=limit, use_graph=use_graph,
                                **knobs)
             acc.add(e.last_stats())
@@ -366,7 +327,7 @@ def run_ours(args, dist):
         for i in range(args.warmup):
             step(i, batches[i % len(batches)], StepStats(), warm)
         if feed:
-            feed.flush(StepStats(), warm)
+            feed.flush(warm)
         dist.barrier()
         cuda_sync()
         acc = StepStats()
@@ -390,7 +351,7 @@ def run_ours(args, dist):
                     f"{st['enum_passes']} passes); tasks {st['enum_tasks']} pops {st['enum_pops']} handoffs "
                     f"{st['enum_handoffs']} records {st['enum_records']} examines {st['enum_examines']}")
             if feed:
-                feed.flush(acc, results)
+                feed.flush(results, acc.add)
             cuda_sync()
             wall = time.perf_counter() - t0
         dist.barrier()

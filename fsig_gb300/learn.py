@@ -256,6 +256,53 @@ def train(engine: Engine, data, epochs: int = 60, lr: float = 2e-3, batch_graphs
     return engine.mpnn_get_params(), losses
 
 
+class LearnedFeed:
+    """Serving batches in learned order with the heuristic order as fallback,
+    without a batch of its own per fallback: a query over the work limit is
+    carried into the next batch with its heuristic order attached (a
+    learned-order batch keeps caller-given orders); the ones left after the
+    last batch run together at flush().  step(k, batch, results) writes
+    (count, hash) pairs into results[k]; a carried query's pair is filled in
+    when its later batch returns.  on_stats, when given, receives the engine's
+    statistics after every call."""
+
+    def __init__(self, engine: Engine, algo: int = ALGO_FUSED, work_limit: int = 1 << 26, **kw):
+        self.engine, self.algo, self.work_limit, self.kw = engine, algo, work_limit, kw
+        self.pending = []  # (step, index, query with its heuristic order)
+
+    def _run(self, qs, on_stats):
+        rs = self.engine.match_batch(qs, algo=self.algo, order_source=ORDER_LEARNED, max_work=self.work_limit,
+                                     **self.kw)
+        if on_stats:
+            on_stats(self.engine.last_stats())
+        return rs
+
+    def _settle(self, rs, results):
+        for (k, i, _), r in zip(self.pending, rs):
+            if r.status != 0:
+                raise RuntimeError(f"fallback query failed with status {r.status}")
+            results[k][i] = (r.count, r.hash)
+        self.pending = []
+
+    def step(self, k, batch, results, on_stats=None):
+        """Runs one batch (plus carried queries); returns (its results, fallbacks)."""
+        from . import ALGO_GSI, plan_order
+        rs = self._run(list(batch) + [q for _, _, q in self.pending], on_stats)
+        self._settle(rs[len(batch):], results)
+        rs = rs[: len(batch)]
+        results[k] = [(r.count, r.hash) for r in rs]
+        for i, r in enumerate(rs):
+            if r.status == ELIMIT:
+                order = plan_order(batch[i], ALGO_GSI, r.candidates)["order"]
+                self.pending.append((k, i, Query(batch[i].labels, batch[i].edges,
+                                                 order=np.asarray(order, np.uint32))))
+        return rs, sum(1 for r in rs if r.status == ELIMIT)
+
+    def flush(self, results, on_stats=None):
+        if self.pending:
+            self._settle(self._run([q for _, _, q in self.pending], on_stats), results)
+
+
 def match_learned(engine: Engine, queries: Sequence[Query], algo: int = ALGO_FUSED, work_limit: int = 0, **kw):
     """Batched learned-order matching with the heuristic order as fallback:
     queries that exceed work_limit under the learned order run again with the

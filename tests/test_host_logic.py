@@ -106,20 +106,20 @@ class FeedEngine:
 
 
 def test_fallbacks_ride_along_in_the_next_batch(monkeypatch):
-    import bench
     monkeypatch.setattr(F, "plan_order", lambda q, algo, cand: {"order": [2, 1, 0]})
     eng = FeedEngine()
-    feed = bench.LearnedFeed(eng, F.ALGO_FUSED, 1 << 20, False, {})
+    feed = learn.LearnedFeed(eng, F.ALGO_FUSED, 1 << 20)
+    stats = []
 
     def q(tag):
         return F.Query(np.full(3, tag, np.int32), np.asarray([(0, 1), (1, 2)], np.uint32))
 
     batches = [[q(1), q(99)], [q(2), q(3)]]
     results = [None, None]
-    acc = bench.StepStats()
-    _, fb0 = feed.step(0, batches[0], acc, results)
-    _, fb1 = feed.step(1, batches[1], acc, results)
-    feed.flush(acc, results)
+    _, fb0 = feed.step(0, batches[0], results, stats.append)
+    _, fb1 = feed.step(1, batches[1], results, stats.append)
+    feed.flush(results, stats.append)
     assert (fb0, fb1) == (1, 0)
     assert eng.calls == [[False, False], [False, False, True]]  # the fallback rides in batch 1 with its order
     assert results == [[(1, 10), (99, 990)], [(2, 20), (3, 30)]]
+    assert len(stats) == 2
