@@ -123,7 +123,8 @@ int fsig_graph_info(const fsig_engine* e, uint32_t* num_vertices, uint64_t* num_
 /* Binary cache of the resident graph store (the device arrays as built: the
  * renumbered CSR, caller ids, label segments and signatures), in place of the
  * reference's commented-out binary PCSR dump (graph_format_transformer.cc:47-74,
- * 197-213): a load is a file read and copies, no parsing or building. */
+ * 197-213): a load is a file read and copies, no parsing or building.  A
+ * load replaces the resident graph; when it fails no graph is resident. */
 int fsig_save_graph_cache(fsig_engine* e, const char* path);
 int fsig_load_graph_cache(fsig_engine* e, const char* path);
 
