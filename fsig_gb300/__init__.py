@@ -117,6 +117,8 @@ def engine_library() -> C.CDLL:
     L.fsig_build_signature.argtypes = [vp, C.c_uint32, C.POINTER(C.c_int32), C.POINTER(C.c_uint32),
                                        C.POINTER(C.c_uint32), C.c_int, C.POINTER(C.c_uint32)]
     L.fsig_filter.argtypes = [vp, C.POINTER(_Query), C.c_int, C.c_int, C.POINTER(C.c_uint8)]
+    u32p = C.POINTER(C.c_uint32)
+    L.fsig_build_pcsr.argtypes = [vp, C.c_uint32, C.c_int32, C.POINTER(C.c_int32), u32p, u32p, u32p, u32p, u32p, u32p]
     L.fsig_plan_order.argtypes = [C.POINTER(_Query), C.c_int, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
                                   C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
     L.fsig_last_stats.argtypes = [vp, C.POINTER(_Stats)]
@@ -142,7 +144,7 @@ def engine_library() -> C.CDLL:
     L.fsig_write_embeddings.argtypes = [vp, C.POINTER(_Query), C.c_int, C.c_char_p, C.POINTER(_Result)]
     for name in ("fsig_mpnn_set_params", "fsig_mpnn_get_params", "fsig_mpnn_features", "fsig_mpnn_forward",
                  "fsig_mpnn_train_step", "fsig_read_graph_file", "fsig_read_graph_file_threads", "fsig_save_graph_cache", "fsig_load_graph_cache", "fsig_graph_file_data", "fsig_match_embeddings",
-                 "fsig_write_embeddings", "fsig_filter_noalloc", "fsig_last_stats", "fsig_plan_order", "fsig_create", "fsig_destroy", "fsig_load_graph", "fsig_load_graph_file", "fsig_graph_info",
+                 "fsig_write_embeddings", "fsig_build_pcsr", "fsig_filter_noalloc", "fsig_last_stats", "fsig_plan_order", "fsig_create", "fsig_destroy", "fsig_load_graph", "fsig_load_graph_file", "fsig_graph_info",
                  "fsig_match", "fsig_match_batch", "fsig_build_csr", "fsig_build_signature", "fsig_filter"):
         getattr(L, name).restype = C.c_int
     _eng = L
@@ -486,6 +488,31 @@ class Engine:
         self._check(self._L.fsig_build_signature(self._h, len(lab), _i32p(lab), _u32p(off), _u32p(a),
                                                  1 if column_oriented else 0, _u32p(out)), "build_signature")
         return out
+
+    def build_pcsr(self, labels, offsets, adj, num_labels: int) -> list:
+        """The reference's PCSR units, built on the device: a list of
+        (keys, list entries, slot table, lists) per unit, as the oracle's pcsr()."""
+        lab = np.ascontiguousarray(labels, np.int32)
+        off = np.ascontiguousarray(offsets, np.uint32)
+        a = np.ascontiguousarray(adj, np.uint32)
+        if a.size == 0:
+            a = np.zeros(1, np.uint32)
+        U = num_labels * (num_labels + 1) // 2
+        keys = np.zeros(max(U, 1), np.uint32)
+        ne = np.zeros(max(U, 1), np.uint32)
+        self._check(self._L.fsig_build_pcsr(self._h, len(lab), num_labels, _i32p(lab), _u32p(off), _u32p(a),
+                                            _u32p(keys), _u32p(ne), None, None), "build_pcsr")
+        table = np.zeros(max(int(keys[:U].sum()) * 32, 1), np.uint32)
+        edges = np.zeros(max(int(ne[:U].sum()), 1), np.uint32)
+        self._check(self._L.fsig_build_pcsr(self._h, len(lab), num_labels, _i32p(lab), _u32p(off), _u32p(a),
+                                            _u32p(keys), _u32p(ne), _u32p(table), _u32p(edges)), "build_pcsr")
+        units, ob, eb = [], 0, 0
+        for u in range(U):
+            k, m = int(keys[u]), int(ne[u])
+            units.append((k, m, table[ob: ob + 32 * k].copy(), edges[eb: eb + m].copy()))
+            ob += 32 * k
+            eb += m
+        return units
 
     def filter(self, q: Query, algo: int = ALGO_GSI, refine_iters: int = -1) -> np.ndarray:
         keep = []

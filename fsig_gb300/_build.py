@@ -27,7 +27,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-r
               "-Xptxas", "-warn-spills"]
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-Wall", "-Wno-unused-function"]
 
-ENGINE_SOURCES = ["graph_store.cu", "match.cu", "capi.cu", "mpnn.cu", "plan.cu", "reader.cpp"]
+ENGINE_SOURCES = ["graph_store.cu", "match.cu", "capi.cu", "mpnn.cu", "pcsr.cu", "plan.cu", "reader.cpp"]
 GEN_SOURCES = ["gen.cpp"]
 
 

@@ -482,6 +482,16 @@ int fsig_build_signature(fsig_engine* h, uint32_t V, const int32_t* labels, cons
   return finish(h, fsig::build_reference_signature(h->e, V, labels, offsets, adj, column_oriented, signature));
 }
 
+int fsig_build_pcsr(fsig_engine* h, uint32_t V, int32_t L, const int32_t* labels, const uint32_t* offsets,
+                    const uint32_t* adj, uint32_t* unit_keys, uint32_t* unit_edges, uint32_t* table,
+                    uint32_t* edges) {
+  int rc = select(h);
+  if (rc) return finish(h, rc);
+  if (!labels || !offsets || !unit_keys || !unit_edges || (offsets[V] && !adj))
+    return finish(h, fsig::fail(FSIG_EINVAL, "null argument"));
+  return finish(h, fsig::build_reference_pcsr(h->e, V, L, labels, offsets, adj, unit_keys, unit_edges, table, edges));
+}
+
 int fsig_filter(fsig_engine* h, const fsig_query* q, int algo, int refine_iters, uint8_t* flags) {
   int rc = select(h);
   if (rc) return finish(h, rc);

@@ -62,6 +62,10 @@ struct Engine {
 // graph_store.cu
 int build_device_graph(Engine& e, uint32_t V, const int32_t* labels, uint64_t E, const uint32_t* edges);
 int save_graph_cache(Engine& e, const char* path);
+// pcsr.cu
+int build_reference_pcsr(Engine& e, uint32_t V, int32_t L, const int32_t* labels, const uint32_t* off,
+                         const uint32_t* adj, uint32_t* unit_keys, uint32_t* unit_edges, uint32_t* table,
+                         uint32_t* edges);
 int load_graph_cache(Engine& e, const char* path);
 int build_reference_csr(Engine& e, uint32_t V, uint64_t E, const uint32_t* edges, uint32_t* offsets,
                         uint32_t* adj);

@@ -226,6 +226,16 @@ int fsig_build_csr(fsig_engine* e, uint32_t num_vertices, uint64_t num_edges,
 int fsig_build_signature(fsig_engine* e, uint32_t num_vertices, const int32_t* labels,
                          const uint32_t* offsets, const uint32_t* adj, int column_oriented,
                          uint32_t* signature);
+/* UndirectedPlainToPCSRTransformer::transform (graph_format_transformer.cc:39-215)
+ * over a CSR with labels in [0, num_labels): U = num_labels (num_labels + 1) / 2
+ * units (get_edge_label, graph/graph.h:107-122); unit_keys[U] and unit_edges[U]
+ * give each unit's keys and list entries.  When table and edges are given they
+ * receive every unit's 32-word slot table (32 x keys words) and its lists,
+ * units concatenated in order.  Computed on the device; call once with
+ * table = edges = NULL for the sizes. */
+int fsig_build_pcsr(fsig_engine* e, uint32_t num_vertices, int32_t num_labels, const int32_t* labels,
+                    const uint32_t* offsets, const uint32_t* adj, uint32_t* unit_keys, uint32_t* unit_edges,
+                    uint32_t* table, uint32_t* edges);
 
 /* ---- join order on the host, no device work; replaces GSI::generate_join_order
  *      (match/GSI.cu:105-149, algo 2 and 3) and MMatch::decompose_query_graph +

@@ -328,3 +328,39 @@ def test_graph_cache_round_trip(engine, golden, tmp_path):
     with pytest.raises(F.FsigError) as ei:
         engine.load_graph_cache(tmp_path / "bad.fsigcache")
     assert ei.value.status == F.EIO
+
+
+@pytest.mark.parametrize("name", ["small_l4", "small_l4_trailing_newline", "mid_l8", "cl_zipf16"])
+def test_device_pcsr_matches_reference(engine, golden, name):
+    """The PCSR units built on the device equal the reference's own output
+    (recorded digests) and the oracle's restatement word for word."""
+    import hashlib
+    rec, d = oracle_graph(name, golden)
+    units = engine.build_pcsr(d["labels"], d["offsets"], d["edges"], d["L"])
+    assert len(units) == rec["pcsr_units"]
+
+    def sha(a):
+        return hashlib.sha256(np.ascontiguousarray(a, np.uint32).tobytes()).hexdigest()
+
+    for (k, m, off, e), (rk, rm, roff, re_) in zip(units, rec["pcsr"]):
+        assert (k, m) == (rk, rm)
+        assert sha(off) == roff and sha(e) == re_
+    for (k, m, off, e), (ok, om, ooff, oe) in zip(units, O.pcsr(d["labels"], d["offsets"], d["edges"], d["L"])):
+        assert (k, m) == (ok, om) and np.array_equal(off, ooff) and np.array_equal(e, oe)
+
+
+def test_device_pcsr_with_overflow_chains(engine):
+    """A unit whose bucket gets more than 15 keys, so that its slot chains to
+    the first empty bucket: a star whose 20 leaves all hash to bucket 3 of the
+    unit's 21 keys."""
+    nk = 21
+    leaves = [v for v in range(1, 5000) if O.murmur2_u32(v) % nk == 3][:20]
+    lab = np.zeros(max(leaves) + 1, np.int32)
+    lab[leaves] = 1
+    g = F.Graph(lab, np.array([(0, v) for v in leaves], np.uint32))
+    off, adj = g.csr()
+    ref = O.pcsr(lab, off, adj, 2)
+    assert (ref[0][2].reshape(-1, 32)[:, 30] != 0xFFFFFFFF).sum() == 1  # one chained slot
+    units = engine.build_pcsr(lab, off, adj, 2)
+    for (k, m, o, e), (ok, om, ooff, oe) in zip(units, ref):
+        assert (k, m) == (ok, om) and np.array_equal(o, ooff) and np.array_equal(e, oe)
