@@ -378,6 +378,39 @@ def _as_cquery(q: Query, keep: list) -> _Query:
     return cq
 
 
+_QUERY_DTYPE = np.dtype({"names": ["nv", "ne", "labels", "edges", "order"],
+                          "formats": ["<u4", "<u4", "<u8", "<u8", "<u8"],
+                          "offsets": [0, 4, 8, 16, 24], "itemsize": 32})
+
+
+def _pack_queries(qs: Sequence[Query]):
+    """fsig_query[len(qs)] for a batch, built with a few array operations: the
+    labels, edges and orders of all queries in three arrays, the structs as one
+    structured array pointing into them.  Returns (pointer, arrays to keep)."""
+    n = len(qs)
+    labs = [np.asarray(q.labels, np.int32).reshape(-1) for q in qs]
+    eds = [np.asarray(q.edges, np.uint32).reshape(-1) for q in qs]
+    ords = [np.asarray(q.order, np.uint32).reshape(-1) for q in qs if q.order is not None]
+    lab = np.ascontiguousarray(np.concatenate(labs) if n else np.zeros(0, np.int32), np.int32)
+    edg = np.ascontiguousarray(np.concatenate(eds) if n else np.zeros(0, np.uint32), np.uint32)
+    ordv = np.ascontiguousarray(np.concatenate(ords) if ords else np.zeros(0, np.uint32), np.uint32)
+    nv = np.fromiter((len(x) for x in labs), np.uint64, n)
+    ne2 = np.fromiter((len(x) for x in eds), np.uint64, n)
+    arr = np.zeros(max(n, 1), _QUERY_DTYPE)
+    if n:
+        arr["nv"][:n] = nv
+        arr["ne"][:n] = ne2 // 2
+        lo = np.concatenate([[0], np.cumsum(nv)[:-1]]).astype(np.uint64)
+        eo = np.concatenate([[0], np.cumsum(ne2)[:-1]]).astype(np.uint64)
+        arr["labels"][:n] = np.uint64(lab.ctypes.data) + 4 * lo
+        arr["edges"][:n] = np.where(ne2 > 0, np.uint64(edg.ctypes.data) + 4 * eo, 0)
+        has = np.fromiter((q.order is not None for q in qs), bool, n)
+        if has.any():
+            oo = np.concatenate([[0], np.cumsum(np.where(has, nv, 0))[:-1]]).astype(np.uint64)
+            arr["order"][:n] = np.where(has, np.uint64(ordv.ctypes.data) + 4 * oo, 0)
+    return arr.ctypes.data_as(C.POINTER(_Query)), (arr, lab, edg, ordv)
+
+
 def _result(r: _Result) -> Result:
     n = r.num_vertices
     return Result(int(r.count), int(r.hash), int(r.status), list(r.order[:n]), list(r.candidates[:n]),
@@ -452,10 +485,7 @@ class Engine:
                     refine_iters: int = -1, chunk: int = 0, use_graph: bool = False, split_len: int = 0,
                     split_cycles: int = 0, max_work: int = 0, warps_per_block: int = 0,
                     learned_window: int = 0) -> list:
-        keep = []
-        arr = (_Query * max(len(qs), 1))()
-        for i, q in enumerate(qs):
-            arr[i] = _as_cquery(q, keep)
+        arr, keep = _pack_queries(qs)
         res = (_Result * max(len(qs), 1))()
         opts = _BatchOpts(algo, order_source, refine_iters, 1 if use_graph else 0, chunk, split_len, split_cycles,
                           max_work, warps_per_block, learned_window)

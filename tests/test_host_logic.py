@@ -123,3 +123,26 @@ def test_fallbacks_ride_along_in_the_next_batch(monkeypatch):
     assert eng.calls == [[False, False], [False, False, True]]  # the fallback rides in batch 1 with its order
     assert results == [[(1, 10), (99, 990)], [(2, 20), (3, 30)]]
     assert len(stats) == 2
+
+
+def test_batch_packing_matches_per_query_packing():
+    """The vectorized fsig_query array of a batch points at the same labels,
+    edges and orders as packing each query on its own."""
+    rng = np.random.default_rng(4)
+    qs = []
+    for i in range(40):
+        n = int(rng.integers(1, 33))
+        e = [(j, int(rng.integers(0, j))) for j in range(1, n)]
+        q = F.Query(rng.integers(0, 5, n).astype(np.int32), np.asarray(e, np.uint32).reshape(-1, 2))
+        if i % 3 == 0:
+            q = F.Query(q.labels, q.edges, order=np.arange(n, dtype=np.uint32))
+        qs.append(q)
+    ptr, keep = F._pack_queries(qs)
+    for i, q in enumerate(qs):
+        a = ptr[i]
+        assert (a.num_vertices, a.num_edges) == (q.num_vertices, len(q.edges))
+        assert list(a.labels[:a.num_vertices]) == q.labels.tolist()
+        assert list(a.edges[:2 * a.num_edges]) == np.asarray(q.edges).reshape(-1).tolist()
+        assert bool(a.order) == (q.order is not None)
+        if q.order is not None:
+            assert list(a.order[:a.num_vertices]) == q.order.tolist()
