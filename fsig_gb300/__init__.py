@@ -55,7 +55,8 @@ class _Result(C.Structure):
 class _BatchOpts(C.Structure):
     _fields_ = [("algo", C.c_int), ("order_source", C.c_int), ("refine_iters", C.c_int), ("use_graph", C.c_int),
                 ("chunk", C.c_uint32), ("split_len", C.c_uint32), ("split_cycles", C.c_uint64),
-                ("max_work", C.c_uint64), ("warps_per_block", C.c_uint32), ("learned_window", C.c_uint32)]
+                ("max_work", C.c_uint64), ("warps_per_block", C.c_uint32), ("learned_window", C.c_uint32),
+                ("no_classes", C.c_uint32)]
 
 
 class _Stats(C.Structure):
@@ -117,7 +118,9 @@ def engine_library() -> C.CDLL:
     L.fsig_build_signature.argtypes = [vp, C.c_uint32, C.POINTER(C.c_int32), C.POINTER(C.c_uint32),
                                        C.POINTER(C.c_uint32), C.c_int, C.POINTER(C.c_uint32)]
     L.fsig_filter.argtypes = [vp, C.POINTER(_Query), C.c_int, C.c_int, C.POINTER(C.c_uint8)]
+    L.fsig_filter_classes.argtypes = [vp, C.POINTER(_Query), C.c_int, C.c_int, C.c_int, C.POINTER(C.c_uint8)]
     u32p = C.POINTER(C.c_uint32)
+    L.fsig_refine_classes.argtypes = [C.POINTER(_Query), u32p, u32p]
     L.fsig_build_pcsr.argtypes = [vp, C.c_uint32, C.c_int32, C.POINTER(C.c_int32), u32p, u32p, u32p, u32p, u32p, u32p]
     L.fsig_plan_order.argtypes = [C.POINTER(_Query), C.c_int, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
                                   C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
@@ -145,7 +148,8 @@ def engine_library() -> C.CDLL:
     for name in ("fsig_mpnn_set_params", "fsig_mpnn_get_params", "fsig_mpnn_features", "fsig_mpnn_forward",
                  "fsig_mpnn_train_step", "fsig_read_graph_file", "fsig_read_graph_file_threads", "fsig_save_graph_cache", "fsig_load_graph_cache", "fsig_graph_file_data", "fsig_match_embeddings",
                  "fsig_write_embeddings", "fsig_build_pcsr", "fsig_filter_noalloc", "fsig_last_stats", "fsig_plan_order", "fsig_create", "fsig_destroy", "fsig_load_graph", "fsig_load_graph_file", "fsig_graph_info",
-                 "fsig_match", "fsig_match_batch", "fsig_build_csr", "fsig_build_signature", "fsig_filter"):
+                 "fsig_match", "fsig_match_batch", "fsig_build_csr", "fsig_build_signature", "fsig_filter",
+                 "fsig_filter_classes", "fsig_refine_classes"):
         getattr(L, name).restype = C.c_int
     _eng = L
     return L
@@ -484,11 +488,11 @@ class Engine:
     def match_batch(self, qs: Sequence[Query], algo: int = ALGO_FUSED, order_source: int = ORDER_HEURISTIC,
                     refine_iters: int = -1, chunk: int = 0, use_graph: bool = False, split_len: int = 0,
                     split_cycles: int = 0, max_work: int = 0, warps_per_block: int = 0,
-                    learned_window: int = 0) -> list:
+                    learned_window: int = 0, classes: bool = True) -> list:
         arr, keep = _pack_queries(qs)
         res = (_Result * max(len(qs), 1))()
         opts = _BatchOpts(algo, order_source, refine_iters, 1 if use_graph else 0, chunk, split_len, split_cycles,
-                          max_work, warps_per_block, learned_window)
+                          max_work, warps_per_block, learned_window, 0 if classes else 1)
         self._check(self._L.fsig_match_batch(self._h, len(qs), arr, C.byref(opts), res), "match_batch")
         return [_result(res[i]) for i in range(len(qs))]
 
@@ -544,13 +548,13 @@ class Engine:
             eb += m
         return units
 
-    def filter(self, q: Query, algo: int = ALGO_GSI, refine_iters: int = -1) -> np.ndarray:
+    def filter(self, q: Query, algo: int = ALGO_GSI, refine_iters: int = -1, classes: bool = True) -> np.ndarray:
         keep = []
         cq = _as_cquery(q, keep)
         V = self.graph_info()["V"]
         out = np.zeros(q.num_vertices * V, np.uint8)
-        self._check(self._L.fsig_filter(self._h, C.byref(cq), algo, refine_iters,
-                                        out.ctypes.data_as(C.POINTER(C.c_uint8))), "filter")
+        self._check(self._L.fsig_filter_classes(self._h, C.byref(cq), algo, refine_iters, 1 if classes else 0,
+                                                out.ctypes.data_as(C.POINTER(C.c_uint8))), "filter")
         return out.reshape(q.num_vertices, V)
 
     # embeddings (EmbeddingWriter)
@@ -642,6 +646,24 @@ def plan_order(q: Query, algo: int, candidates) -> dict:
     if rc:
         raise FsigError(rc, "plan_order failed")
     return dict(order=order.tolist(), types=types.tolist(), classes=classes.tolist())
+
+
+def refine_classes(q: Query) -> dict:
+    """Refinement classes of a query (host only): classes[u] = the smallest
+    member of u's class; dominated[u] = a class whose candidate set contains
+    u's class's (FSIG_NO_CLASS = 255: none, and for every non-smallest member)."""
+    keep = []
+    cq = _as_cquery(q, keep)
+    n = q.num_vertices
+    classes = np.zeros(n, np.uint32)
+    dominated = np.zeros(n, np.uint32)
+    rc = engine_library().fsig_refine_classes(C.byref(cq), _u32p(classes), _u32p(dominated))
+    if rc:
+        raise FsigError(rc, "refine_classes failed")
+    return dict(classes=classes.tolist(), dominated=dominated.tolist())
+
+
+NO_CLASS = 0xFF
 
 
 def select_within_budget(engine: "Engine", candidates: Sequence[Query], want: int, max_work: int,

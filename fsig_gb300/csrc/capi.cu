@@ -352,7 +352,7 @@ int fsig_match_batch(fsig_engine* h, uint32_t nq, const fsig_query* qs, const fs
   int rc = select(h);
   if (rc) return finish(h, rc);
   if ((nq && (!qs || !out))) return finish(h, fsig::fail(FSIG_EINVAL, "null argument"));
-  fsig_batch_opts def{FSIG_ALGO_FUSED, FSIG_ORDER_HEURISTIC, -1, 0, 0, 0, 0, 0, 0, 0};
+  fsig_batch_opts def{FSIG_ALGO_FUSED, FSIG_ORDER_HEURISTIC, -1, 0, 0, 0, 0, 0, 0, 0, 0};
   const fsig_batch_opts& bo = opts ? *opts : def;
   if (bo.algo != FSIG_ALGO_FSIG && bo.algo != FSIG_ALGO_GSI && bo.algo != FSIG_ALGO_FUSED)
     return finish(h, fsig::fail(FSIG_EINVAL, "unknown algorithm"));
@@ -376,6 +376,7 @@ int fsig_match_batch(fsig_engine* h, uint32_t nq, const fsig_query* qs, const fs
     o.learned = true;
   }
   o.use_graph = bo.use_graph != 0;
+  o.classes = bo.no_classes == 0;
   if (bo.learned_window) o.learned_window = bo.learned_window;
   if (bo.warps_per_block) {
     if (bo.warps_per_block > fsig::kEnumWarps) return finish(h, fsig::fail(FSIG_EINVAL, "warps_per_block too large"));
@@ -492,7 +493,8 @@ int fsig_build_pcsr(fsig_engine* h, uint32_t V, int32_t L, const int32_t* labels
   return finish(h, fsig::build_reference_pcsr(h->e, V, L, labels, offsets, adj, unit_keys, unit_edges, table, edges));
 }
 
-int fsig_filter(fsig_engine* h, const fsig_query* q, int algo, int refine_iters, uint8_t* flags) {
+int fsig_filter_classes(fsig_engine* h, const fsig_query* q, int algo, int refine_iters, int classes,
+                        uint8_t* flags) {
   int rc = select(h);
   if (rc) return finish(h, rc);
   if (!q || !flags) return finish(h, fsig::fail(FSIG_EINVAL, "null argument"));
@@ -501,7 +503,26 @@ int fsig_filter(fsig_engine* h, const fsig_query* q, int algo, int refine_iters,
   if (rc) return finish(h, rc);
   fsig::BatchOptions o;
   algo_options(algo, refine_iters, o);
-  return finish(h, fsig::run_filter_probe(h->e, hq, o.filter_mode, o.refine_iters, flags));
+  return finish(h, fsig::run_filter_probe(h->e, hq, o.filter_mode, o.refine_iters, classes != 0, flags));
+}
+
+int fsig_filter(fsig_engine* h, const fsig_query* q, int algo, int refine_iters, uint8_t* flags) {
+  return fsig_filter_classes(h, q, algo, refine_iters, 1, flags);
+}
+
+int fsig_refine_classes(const fsig_query* q, uint32_t* classes, uint32_t* dominated) {
+  fsig::clear_thread_error();
+  if (!q) return FSIG_EINVAL;
+  fsig::HostQuery hq;
+  int rc = fsig::prepare_query(*q, 0, hq);
+  if (rc) return rc;
+  uint8_t c[fsig::kMaxQ], d[fsig::kMaxQ];
+  fsig::refine_classes(hq, c, d);
+  for (uint32_t u = 0; u < hq.n; u++) {
+    if (classes) classes[u] = c[u];
+    if (dominated) dominated[u] = d[u];
+  }
+  return FSIG_OK;
 }
 
 // Allocation-free filter: the arena is not touched; see run_filter_noalloc.

@@ -94,9 +94,18 @@ __global__ void __launch_bounds__(256) filter_kernel(GraphView g, const QVert* _
 }
 
 // ---------------------------------------------------------------------------
-// One Jacobi step of neighbour-support refinement: v stays in C(u) only if for
-// every query neighbour w of u some neighbour of v (in the label-l(w) segment)
-// is in C(w) as read from src.  Warps take runs of bitmap words.
+// One Jacobi step of neighbour-support refinement.  The query neighbours of u
+// are grouped by refinement class; v stays in C(u) only if, for every group
+// of k neighbours in class y, at least k entries of v's label-l(y) neighbour
+// segment are in C(y) as read from src (k distinct query neighbours need k
+// distinct data neighbours; the count of entries with repeated edges is an
+// upper bound, so the test never drops a true image).  This is the pull-mode
+// check of MMatch (count_neighbors_kernel + check_re_kernel,
+// MMatch_kernels.cuh:28-117, 190-214) with its per-class thresholds.  With
+// every vertex its own class every k is one.  A class dominated by u's (dom)
+// is tested first: C(u) stays within C(dom) through the refinement, so a v
+// outside C(dom) fails one of the counts anyway.  Warps take runs of bitmap
+// words; class members other than the smallest own no words.
 // ---------------------------------------------------------------------------
 constexpr uint32_t kRefineRun = 8;
 
@@ -125,14 +134,25 @@ __global__ void __launch_bounds__(256) refine_kernel(GraphView g, const QVert* _
         if (lane == 0) dst[W] = word;
         continue;
       }
-      const uint32_t v = q->bmbase + uint32_t((W - q->bmoff) << 5) + lane;
+      const uint32_t bit0 = uint32_t((W - q->bmoff) << 5) + lane;  // bit of v in every bitmap of u's label
+      const uint32_t v = q->bmbase + bit0;
       bool alive = (word >> lane) & 1u;
-      uint32_t m = q->adj;
       const uint32_t gbase = gi - q->u;
-      while (m) {
+      if (q->dom != kNoClass) {
+        const QVert* qd = qv + gbase + q->dom;
+        alive = alive && ((src[qd->bmoff + (bit0 >> 5)] >> (bit0 & 31)) & 1u);
+      }
+      uint32_t m = q->adj;
+      while (m && __any_sync(kFull, alive)) {
         const uint32_t wv = __ffs(m) - 1;
-        m &= m - 1;
         const QVert* qw = qv + gbase + wv;
+        uint32_t grp = 0;
+        for (uint32_t r = m; r; r &= r - 1) {
+          const uint32_t x = __ffs(r) - 1;
+          if (qv[gbase + x].cls == qw->cls) grp |= 1u << x;
+        }
+        m &= ~grp;
+        const uint32_t need = __popc(grp);
         if (alive) {
           if (qw->words == 0) {
             alive = false;
@@ -140,12 +160,12 @@ __global__ void __launch_bounds__(256) refine_kernel(GraphView g, const QVert* _
             const uint32_t* s = g.lseg + uint64_t(v) * W1 + qw->label;
             uint32_t k = s[0];
             const uint32_t e = s[1];
-            bool found = false;
-            for (; k < e; k++) {
+            uint32_t have = 0;
+            for (; k < e && have < need; k++) {
               const uint32_t bit = g.adj[k] - qw->bmbase;
-              if ((src[qw->bmoff + (bit >> 5)] >> (bit & 31)) & 1u) { found = true; break; }
+              have += (src[qw->bmoff + (bit >> 5)] >> (bit & 31)) & 1u;
             }
-            alive = found;
+            alive = have >= need;
           }
         }
       }
@@ -439,7 +459,10 @@ struct BatchLayout {
   std::vector<uint64_t> gword;
 };
 
-void layout_batch(const DeviceGraph& g, const std::vector<HostQuery>& qs, BatchLayout& b) {
+// Bitmap layout of a batch: one bitmap per query vertex over its label's id
+// range, except that members of a refinement class (classes on) use the
+// bitmap of the class's smallest member and own no words.
+void layout_batch(const DeviceGraph& g, const std::vector<HostQuery>& qs, BatchLayout& b, bool classes) {
   b.Q = uint32_t(qs.size());
   b.qoff.assign(size_t(b.Q) + 1, 0);
   for (uint32_t q = 0; q < b.Q; q++) b.qoff[q + 1] = b.qoff[q] + qs[q].n;
@@ -451,6 +474,12 @@ void layout_batch(const DeviceGraph& g, const std::vector<HostQuery>& qs, BatchL
   for (uint32_t q = 0; q < b.Q; q++) {
     const HostQuery& h = qs[q];
     uint64_t qmax = 0;
+    uint8_t cls[kMaxQ], dom[kMaxQ];
+    if (classes) {
+      refine_classes(h, cls, dom);
+    } else {
+      for (uint32_t u = 0; u < h.n; u++) { cls[u] = uint8_t(u); dom[u] = uint8_t(kNoClass); }
+    }
     for (uint32_t u = 0; u < h.n; u++) {
       const uint32_t gi = b.qoff[q] + u;
       QVert& x = b.qv[gi];
@@ -460,21 +489,28 @@ void layout_batch(const DeviceGraph& g, const std::vector<HostQuery>& qs, BatchL
       x.adj = h.adj[u];
       x.q = q;
       x.u = u;
+      x.cls = cls[u];
+      x.dom = dom[u];
       std::memcpy(x.sig, h.sig[u], sizeof(x.sig));
       const int32_t l = h.label[u];
       uint32_t lo = 0, hi = 0;
       if (l >= 0 && l < g.L) { lo = g.h_base[l]; hi = g.h_base[l + 1]; }
+      b.gword[gi] = w;
       if (hi > lo) {
         x.bmbase = lo & ~31u;
         x.words = ((hi + 31) >> 5) - (lo >> 5);
-        by_label[size_t(l)].push_back(gi);
         qmax = std::max<uint64_t>(qmax, hi - lo);
+        if (cls[u] != u) {  // same label, so the same extent as the class's bitmap
+          x.alias = 1;
+          x.bmoff = b.qv[b.qoff[q] + cls[u]].bmoff;
+          continue;
+        }
+        by_label[size_t(l)].push_back(gi);
       } else {
         x.bmbase = 0;
         x.words = 0;
       }
       x.bmoff = w;
-      b.gword[gi] = w;
       w += x.words;
     }
     rc += qmax;
@@ -772,7 +808,7 @@ int run_batch(Engine& e, const std::vector<HostQuery>& qs, const BatchOptions& o
   const DeviceGraph& g = e.g;
   cudaStream_t s = e.stream;
   BatchLayout b;
-  layout_batch(g, qs, b);
+  layout_batch(g, qs, b, opt.classes);
   const uint32_t Q = b.Q;
   out.res.assign(Q, QueryResult());
   out.counts.assign(b.G, 0);
@@ -1158,7 +1194,7 @@ int run_features(Engine& e, const std::vector<HostQuery>& qs, const uint32_t* co
                  float* features) {
   if (!e.has_graph) return fail(FSIG_ENOGRAPH, "no data graph loaded");
   BatchLayout b;
-  layout_batch(e.g, qs, b);
+  layout_batch(e.g, qs, b, false);
   const uint64_t mark = e.arena.mark();
   int rc = FSIG_OK;
   QVert* d_qv = upload(e, b.qv, rc);
@@ -1188,12 +1224,13 @@ int run_features(Engine& e, const std::vector<HostQuery>& qs, const uint32_t* co
   return FSIG_OK;
 }
 
-int run_filter_probe(Engine& e, const HostQuery& q, uint32_t filter_mode, int refine_iters, uint8_t* flags) {
+int run_filter_probe(Engine& e, const HostQuery& q, uint32_t filter_mode, int refine_iters, bool classes,
+                     uint8_t* flags) {
   if (!e.has_graph) return fail(FSIG_ENOGRAPH, "no data graph loaded");
   const DeviceGraph& g = e.g;
   std::vector<HostQuery> qs(1, q);
   BatchLayout b;
-  layout_batch(g, qs, b);
+  layout_batch(g, qs, b, classes);
   e.arena.release(g.arena_mark);
   int rc = FSIG_OK;
   QVert* d_qv = upload(e, b.qv, rc);
@@ -1326,6 +1363,8 @@ int run_filter_noalloc(Engine& e, const fsig_query& q, uint32_t filter_mode, uin
     x.adj = adj[u];
     x.deg = uint32_t(__builtin_popcount(adj[u]));
     x.u = u;
+    x.cls = uint8_t(u);
+    x.dom = uint8_t(kNoClass);
     x.sig[0] = uint32_t(x.label);
     for (uint32_t w = 0; w < n; w++) {
       if (!((adj[u] >> w) & 1u)) continue;

@@ -9,6 +9,7 @@
 namespace fsig {
 
 constexpr int kMaxQ = FSIG_MAX_QUERY;
+constexpr uint32_t kNoClass = FSIG_NO_CLASS;  // no dominated class
 
 // Filter tests (bit flags).
 constexpr uint32_t kFilterDegree = 1u;
@@ -49,7 +50,10 @@ struct alignas(16) QVert {
   uint32_t u;          // local id
   uint32_t words;      // bitmap words (0: no data vertex carries this label)
   uint32_t bmbase;     // first new id covered by bitmap word 0 (multiple of 32)
-  uint32_t pad;
+  uint8_t cls;         // refinement class: local id of its smallest member
+  uint8_t dom;         // class whose candidate set contains this class's (kNoClass: none)
+  uint8_t alias;       // 1: uses the bitmap of vertex cls (no words of its own)
+  uint8_t pad;
   uint64_t bmoff;      // word offset of the bitmap in the pool
 };
 
@@ -93,6 +97,11 @@ struct BatchOptions {
   const float* scores = nullptr;  // host scores per query vertex (kOrderScores), batch order
   bool learned = false;           // score with the loaded order network (kOrderScores)
   uint32_t learned_window = 32;   // positions a vertex may move from the heuristic order (32: any)
+  // Refinement classes (refine_classes): members share one bitmap, a vertex
+  // needs as many data neighbours in a query neighbour class as it has query
+  // neighbours there, and dominated classes are tested first.  Off: every
+  // vertex its own class (per-vertex support, every count one).
+  bool classes = true;
   // Single-query batches only: write up to emit_cap embeddings to
   // BatchOutput::rows, and enumerate only pass-0 tasks [task_begin, task_end).
   uint64_t emit_cap = 0;
@@ -138,7 +147,8 @@ int run_features(Engine& e, const std::vector<HostQuery>& qs, const uint32_t* co
                  float* features);
 
 // Filter (+ refinement) only; flags[n*V] in caller vertex ids, for one query.
-int run_filter_probe(Engine& e, const HostQuery& q, uint32_t filter_mode, int refine_iters, uint8_t* flags);
+int run_filter_probe(Engine& e, const HostQuery& q, uint32_t filter_mode, int refine_iters, bool classes,
+                     uint8_t* flags);
 
 // Filter without any allocation: bitmaps in a fixed device array, flags
 // written to the caller's device buffer (n * V bytes).
@@ -148,5 +158,7 @@ int run_filter_noalloc(Engine& e, const fsig_query& q, uint32_t filter_mode, uin
 void gsi_order_host(const HostQuery& q, const uint32_t* cand, uint32_t* order);
 void mmatch_order_host(const HostQuery& q, const uint32_t* cand, uint32_t* order);
 void mmatch_structure(const HostQuery& q, uint32_t* types, uint32_t* classes);
+// Refinement classes and dominated classes of one query (kNoClass: none).
+void refine_classes(const HostQuery& q, uint8_t* cls, uint8_t* dom);
 
 }  // namespace fsig

@@ -253,4 +253,81 @@ void mmatch_order_host(const HostQuery& q, const uint32_t* cand, uint32_t* order
   }
 }
 
+// Refinement classes: the coarsest partition of the query vertices that keeps
+// apart vertices whose filter inputs differ (label, degree, signature) and is
+// equitable (members of a class have as many query neighbours as each other
+// in every class).  MMatch::find_equivalent_classes (match/MMatch.cu:44-173)
+// looks for such classes with a permutation search over each vertex's
+// neighbours; colour refinement reaches the coarsest one in polynomial time:
+// each round splits the classes by the multiset of neighbour classes, until a
+// round splits nothing.  Members of a class then have equal candidate sets
+// after the filter and after every refinement step (by induction on the
+// steps), so they share one bitmap.  cls[u] = the smallest member of u's class.
+//
+// dom[u], for a class's smallest member u: a class j != cls[u] of the same
+// label with degree and signature bits within u's and at most as many
+// neighbours as u in every class (the most constrained such j, lowest id on
+// ties), else kNoClass.  Every condition on j is then implied by one on u, so
+// C(u) stays within C(j) through the refinement, and a test of v in C(j)
+// rejects early without changing any outcome (the optimised operators of
+// MMatch::generate_refine_plan, match/MMatch.cu:317-541).
+void refine_classes(const HostQuery& q, uint8_t* cls, uint8_t* dom) {
+  const uint32_t n = q.n;
+  uint32_t col[kMaxQ], next[kMaxQ], members[kMaxQ], reps;
+  for (uint32_t u = 0; u < n; u++) {
+    col[u] = u;
+    for (uint32_t v = 0; v < u; v++)
+      if (q.label[v] == q.label[u] && q.deg[v] == q.deg[u] &&
+          std::memcmp(q.sig[v], q.sig[u], sizeof(q.sig[u])) == 0) {
+        col[u] = v;
+        break;
+      }
+  }
+  // neighbours of u in the class with member mask m
+  auto in_class = [&](uint32_t u, uint32_t m) { return uint32_t(__builtin_popcount(q.adj[u] & m)); };
+  for (;;) {
+    reps = 0;
+    for (uint32_t u = 0; u < n; u++) members[u] = 0;
+    for (uint32_t u = 0; u < n; u++) {
+      members[col[u]] |= 1u << u;
+      if (col[u] == u) reps |= 1u << u;
+    }
+    bool split = false;
+    for (uint32_t u = 0; u < n; u++) {
+      next[u] = u;
+      for (uint32_t v = 0; v < u; v++) {
+        if (col[v] != col[u]) continue;
+        bool same = true;
+        for (uint32_t r = reps; r && same; r &= r - 1) {
+          const uint32_t m = members[__builtin_ctz(r)];
+          same = in_class(u, m) == in_class(v, m);
+        }
+        if (same) { next[u] = v; break; }
+      }
+      split |= next[u] != col[u];
+    }
+    for (uint32_t u = 0; u < n; u++) col[u] = next[u];
+    if (!split) break;
+  }
+  for (uint32_t u = 0; u < n; u++) {
+    cls[u] = uint8_t(col[u]);
+    dom[u] = uint8_t(kNoClass);
+    if (col[u] != u) continue;
+    uint32_t best = kNoClass;
+    for (uint32_t r = reps; r; r &= r - 1) {
+      const uint32_t j = __builtin_ctz(r);
+      if (j == u || q.label[j] != q.label[u] || q.deg[j] > q.deg[u]) continue;
+      if (best != kNoClass && q.deg[j] <= q.deg[best]) continue;
+      bool implied = true;
+      for (int k = 1; k < kSigWords && implied; k++) implied = (q.sig[j][k] & ~q.sig[u][k]) == 0;
+      for (uint32_t y = reps; y && implied; y &= y - 1) {
+        const uint32_t m = members[__builtin_ctz(y)];
+        implied = in_class(j, m) <= in_class(u, m);
+      }
+      if (implied) best = j;
+    }
+    dom[u] = uint8_t(best);
+  }
+}
+
 }  // namespace fsig

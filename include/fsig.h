@@ -98,6 +98,9 @@ typedef struct {
   uint32_t warps_per_block; /* enumeration block size in warps, 1..8 (0: default 8) */
   uint32_t learned_window;  /* FSIG_ORDER_LEARNED: positions a vertex may move away
                                from the heuristic order (0: any)                 */
+  uint32_t no_classes;      /* 1: filter and refine every query vertex on its own,
+                               with every neighbour count one; 0 (default):
+                               refinement classes (see fsig_refine_classes)      */
 } fsig_batch_opts;
 
 /* ---- engine lifetime; replaces GPUSubgraphMatcher::init_GPU (match/subgraph_match.h:51-80)
@@ -247,10 +250,30 @@ int fsig_build_pcsr(fsig_engine* e, uint32_t num_vertices, int32_t num_labels, c
 int fsig_plan_order(const fsig_query* q, int algo, const uint32_t* candidates, uint32_t* order,
                     uint32_t* vertex_types, uint32_t* classes);
 
+/* ---- refinement classes of a query, no device work; the classes of
+ *      MMatch::find_equivalent_classes (match/MMatch.cu:44-173) as the coarsest
+ *      partition that keeps apart vertices of different label, degree or
+ *      signature and in which members of a class have as many neighbours as
+ *      each other in every class.  Members share one candidate bitmap; a
+ *      vertex keeps candidate v only while v has at least k data neighbours
+ *      in C(y) for each class y holding k of its query neighbours (the
+ *      thresholds of MMatch's refine plan, match/MMatch.cu:317-541).
+ *      classes[u] = the smallest member of u's class.  dominated[u] (for the
+ *      smallest member of a class, else FSIG_NO_CLASS): a class whose every
+ *      condition is implied by u's, so C(u) stays within it and the
+ *      refinement tests it first (MMatch's optimised operators); FSIG_NO_CLASS
+ *      when there is none.  Either output may be NULL. ---- */
+#define FSIG_NO_CLASS 0xffu
+int fsig_refine_classes(const fsig_query* q, uint32_t* classes, uint32_t* dominated);
+
 /* ---- candidate filter probe: signature_filter (match/GSI.cu:34-103) and
  *      kernel_initialise + refinement (match/MMatch.cu:609-1227) on the loaded graph.
- *      flags[n * V] (1 = candidate), in the caller's vertex ids. ---- */
+ *      flags[n * V] (1 = candidate), in the caller's vertex ids.  fsig_filter
+ *      refines with refinement classes; fsig_filter_classes chooses
+ *      (classes = 0: every vertex its own class, every neighbour count one). ---- */
 int fsig_filter(fsig_engine* e, const fsig_query* q, int algo, int refine_iters, uint8_t* flags);
+int fsig_filter_classes(fsig_engine* e, const fsig_query* q, int algo, int refine_iters, int classes,
+                        uint8_t* flags);
 
 /* ---- candidate filter that allocates nothing (no counterpart in the reference).
  *      For callers that cannot allocate device memory when they filter: a

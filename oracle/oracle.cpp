@@ -374,24 +374,46 @@ uint64_t orc_simplify(uint32_t V, const uint32_t* off, const uint32_t* adj, uint
   return w;
 }
 
-// Neighbour-support refinement, one Jacobi step per iteration: v stays in
-// C(u) only if, for every query neighbour w of u, some data neighbour of v is
-// in C(w) as it stood at the start of the step.  This is the pull-mode check
-// of MMatch (count_neighbors_kernel + check_re_kernel, MMatch_kernels.cuh:28-117,
-// 190-214) with every required count equal to one.
+// Neighbour-support refinement, one Jacobi step per iteration, with
+// per-class thresholds: u's query neighbours are grouped by class (cls[w],
+// null = every vertex its own class); for each group S, v stays in C(u) only
+// if some data neighbour of v is in C(w) for every w in S, and at least |S|
+// adjacency entries of v are in the union of C(w), w in S, as they stood at
+// the start of the step.  This is the pull-mode check of MMatch
+// (count_neighbors_kernel + check_re_kernel, MMatch_kernels.cuh:28-117,
+// 190-214) with the class counts of its refine plan (MMatch.cu:317-541) as
+// the thresholds; with every vertex its own class every threshold is one.
 void orc_refine(uint32_t V, const int32_t* labels, const uint32_t* off, const uint32_t* adj,
-                uint32_t n, const uint32_t* qadj, int iterations, uint8_t* cand) {
+                uint32_t n, const uint32_t* qadj, const uint32_t* cls, int iterations, uint8_t* cand) {
   (void)labels;
   std::vector<uint8_t> next(size_t(n) * V);
   for (int it = 0; it < iterations; it++) {
     for (uint32_t u = 0; u < n; u++) {
+      // groups of u's neighbours
+      std::vector<std::vector<uint32_t>> groups;
+      for (uint32_t w = 0; w < n; w++) {
+        if (!((qadj[u] >> w) & 1u)) continue;
+        bool placed = false;
+        for (auto& gr : groups)
+          if (cls && cls[gr[0]] == cls[w]) { gr.push_back(w); placed = true; break; }
+        if (!placed) groups.push_back(std::vector<uint32_t>(1, w));
+      }
       for (uint32_t v = 0; v < V; v++) {
         uint8_t keep = cand[size_t(u) * V + v];
-        for (uint32_t w = 0; keep && w < n; w++) {
-          if (!((qadj[u] >> w) & 1u)) continue;
-          bool found = false;
-          for (uint32_t e = off[v]; e < off[v + 1] && !found; e++) found = cand[size_t(w) * V + adj[e]] != 0;
-          keep = found;
+        for (size_t gi = 0; keep && gi < groups.size(); gi++) {
+          const std::vector<uint32_t>& gr = groups[gi];
+          uint64_t in_union = 0;
+          for (uint32_t e = off[v]; e < off[v + 1]; e++) {
+            bool any = false;
+            for (uint32_t w : gr) any = any || cand[size_t(w) * V + adj[e]] != 0;
+            in_union += any ? 1 : 0;
+          }
+          keep = in_union >= gr.size();
+          for (uint32_t w : gr) {
+            bool found = false;
+            for (uint32_t e = off[v]; e < off[v + 1] && !found; e++) found = cand[size_t(w) * V + adj[e]] != 0;
+            keep = keep && found;
+          }
         }
         next[size_t(u) * V + v] = keep;
       }

@@ -66,8 +66,9 @@ uint64_t orc_simplify(uint32_t V, const uint32_t* offsets, const uint32_t* edges
 
 // ---- candidate refinement (Jacobi iterations of the neighbour-support rule) ----
 // cand: n x V flags, in/out.  qadj_mask[u] = bitmask of u's query neighbours.
+// classes[u] = u's refinement class (null: every vertex its own class).
 void orc_refine(uint32_t V, const int32_t* labels, const uint32_t* offsets, const uint32_t* edges,
-                uint32_t n, const uint32_t* qadj_mask, int iterations, uint8_t* cand);
+                uint32_t n, const uint32_t* qadj_mask, const uint32_t* classes, int iterations, uint8_t* cand);
 
 // ---- matcher ----
 // Counts injective label-preserving embeddings of the query (n <= 32 vertices,

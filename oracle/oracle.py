@@ -51,7 +51,7 @@ def _load():
     L.orc_mmatch_init.argtypes = [C.c_uint32, i32p, u32p, C.c_int32, C.c_uint32, u8p]
     L.orc_simplify.restype = C.c_uint64
     L.orc_simplify.argtypes = [C.c_uint32, u32p, u32p, u32p, u32p]
-    L.orc_refine.argtypes = [C.c_uint32, i32p, u32p, u32p, C.c_uint32, u32p, C.c_int, u8p]
+    L.orc_refine.argtypes = [C.c_uint32, i32p, u32p, u32p, C.c_uint32, u32p, C.c_void_p, C.c_int, u8p]
     L.orc_match.restype = C.c_int
     L.orc_match.argtypes = [C.c_uint32, i32p, u32p, u32p, C.c_uint32, i32p, C.c_uint32, u32p, C.c_void_p, C.c_int,
                             C.c_uint64, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), u64p]
@@ -152,16 +152,50 @@ def simplify(offsets, edges):
     return oo, oe[:n]
 
 
-def refine(labels, offsets, edges, qadj_mask, cand, iterations):
+def refine(labels, offsets, edges, qadj_mask, cand, iterations, classes=None):
+    """Refined candidate flags; classes[u] groups u's query neighbours
+    (None: every vertex its own class, every threshold one)."""
     cand = np.ascontiguousarray(cand, np.uint8).copy()
     n = len(qadj_mask)
     V = len(labels)
     e = np.ascontiguousarray(edges, np.uint32)
     if e.size == 0:
         e = np.zeros(1, np.uint32)
+    cls = None if classes is None else np.ascontiguousarray(classes, np.uint32)
     _load().orc_refine(V, np.ascontiguousarray(labels, np.int32), np.ascontiguousarray(offsets, np.uint32), e, n,
-                       np.ascontiguousarray(qadj_mask, np.uint32), int(iterations), cand.reshape(-1))
+                       np.ascontiguousarray(qadj_mask, np.uint32),
+                       None if cls is None else cls.ctypes.data_as(C.c_void_p), int(iterations),
+                       cand.reshape(-1))
     return cand
+
+
+def query_signature(qlabels, qadj_mask):
+    """Signatures of the query vertices over their distinct neighbours, by the
+    data-graph rule (graph_format_transformer.cc:217-262); [n, 16]."""
+    n = len(qlabels)
+    rows = [[w for w in range(n) if (int(qadj_mask[u]) >> w) & 1] for u in range(n)]
+    off = np.zeros(n + 1, np.uint32)
+    off[1:] = np.cumsum([len(r) for r in rows])
+    adj = np.array([w for r in rows for w in r], np.uint32)
+    return signature(qlabels, off, adj).reshape(n, 16)
+
+
+def refine_classes(qlabels, qadj_mask):
+    """Refinement classes: the coarsest partition of the query vertices that
+    keeps apart vertices of different (label, degree, signature) and in which
+    members of a class have the same multiset of neighbour classes (colour
+    refinement to a fixpoint).  classes[u] = the smallest member of u's class."""
+    n = len(qlabels)
+    sig = query_signature(qlabels, qadj_mask)
+    nbrs = [[w for w in range(n) if (int(qadj_mask[u]) >> w) & 1] for u in range(n)]
+    key0 = [(int(qlabels[u]), len(nbrs[u]), tuple(int(x) for x in sig[u])) for u in range(n)]
+    col = [min(v for v in range(n) if key0[v] == key0[u]) for u in range(n)]
+    while True:
+        key = [(col[u], tuple(sorted(col[w] for w in nbrs[u]))) for u in range(n)]
+        new = [min(v for v in range(n) if key[v] == key[u]) for u in range(n)]
+        if new == col:
+            return col
+        col = new
 
 
 def match(labels, offsets, edges, qlabels, qedges, order=None, threads=0, seed=None):

@@ -64,8 +64,13 @@ def query_masks(q):
     return m
 
 
+@pytest.mark.parametrize("classes", [True, False])
 @pytest.mark.parametrize("refine", [0, 1, 3])
-def test_filters_match_oracle(engine, golden, refine):
+def test_filters_match_oracle(engine, golden, refine, classes):
+    """Bit-exact flags.  With classes the members of a class share one
+    bitmap, the thresholds are the class counts and dominated classes are
+    tested first; the oracle has none of the sharing or early tests, only the
+    rule, so equal flags show those change no outcome."""
     g, lab, off, adj = load_simple(engine, "cl_zipf16", golden)
     dsig = O.signature(lab, off, adj, 0)
     for q in golden_queries(golden):
@@ -77,9 +82,10 @@ def test_filters_match_oracle(engine, golden, refine):
         mm = np.stack([O.mmatch_init(lab, off, q.labels[u], qdeg[u]) for u in range(q.num_vertices)])
         fused = gsi & mm
         masks = query_masks(q)
+        cls = O.refine_classes(q.labels, masks) if classes else None
         for algo, base in ((F.ALGO_GSI, gsi), (F.ALGO_FSIG, mm), (F.ALGO_FUSED, fused)):
-            want = O.refine(lab, off, adj, masks, base, refine) if refine else base
-            got = engine.filter(q, algo, refine)
+            want = O.refine(lab, off, adj, masks, base, refine, cls) if refine else base
+            got = engine.filter(q, algo, refine, classes=classes)
             assert np.array_equal(got, want), (algo, refine)
 
 
@@ -289,6 +295,40 @@ def test_work_splitting_preserves_results(engine, config2_small):
         assert [(x.count, x.hash, x.level_counts) for x in r] == [(x.count, x.hash, x.level_counts) for x in base]
     single = [engine.match_batch([q], algo=F.ALGO_FUSED, split_cycles=2000, split_len=32)[0] for q in qs[:6]]
     assert [(x.count, x.hash) for x in single] == [(x.count, x.hash) for x in base[:6]]
+
+
+@pytest.mark.parametrize("algo", [F.ALGO_FSIG, F.ALGO_GSI, F.ALGO_FUSED])
+def test_refinement_classes_change_no_result(engine, config2_small, golden, algo):
+    """Refinement with classes (shared bitmaps, class thresholds, dominated
+    classes tested first) against per-vertex refinement: the same count and
+    hash for every query, never more candidates, and the class thresholds
+    prune somewhere."""
+    g, off, adj, qs = config2_small
+    engine.load_graph(g)
+    fewer = 0
+    for refine in (-1, 3):
+        on = engine.match_batch(qs, algo=algo, refine_iters=refine)
+        off_ = engine.match_batch(qs, algo=algo, refine_iters=refine, classes=False)
+        for a, b, q in zip(on, off_, qs):
+            assert (a.count, a.hash) == (b.count, b.hash)
+            n = q.num_vertices
+            assert all(x <= y for x, y in zip(a.candidates[:n], b.candidates[:n]))
+            fewer += sum(a.candidates[:n]) < sum(b.candidates[:n])
+    sym = [F.Query(np.zeros(k, np.int32), np.array([(i, (i + 1) % k) for i in range(k)], np.uint32))
+           for k in (4, 5, 6)]
+    sym.append(F.Query(np.array([0, 1, 1, 1, 1], np.int32), np.array([(0, i) for i in range(1, 5)], np.uint32)))
+    gl, lab, offs, adjs = load_simple(engine, "cl_zipf16", golden)
+    for q in sym + golden_queries(golden, 8):
+        a = engine.match_batch([q], algo=algo, refine_iters=3)[0]
+        b = engine.match_batch([q], algo=algo, refine_iters=3, classes=False)[0]
+        assert (a.count, a.hash) == (b.count, b.hash)
+        n = q.num_vertices
+        assert all(x <= y for x, y in zip(a.candidates[:n], b.candidates[:n]))
+        fewer += sum(a.candidates[:n]) < sum(b.candidates[:n])
+        if a.count <= 2_000_000:
+            c, h, _ = O.match(lab, offs, adjs, q.labels, q.edges)
+            assert (a.count, a.hash) == (c, h)
+    assert fewer > 0
 
 
 @pytest.mark.parametrize("algo", [F.ALGO_FSIG, F.ALGO_GSI, F.ALGO_FUSED])
