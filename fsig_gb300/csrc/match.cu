@@ -146,11 +146,7 @@ __global__ void __launch_bounds__(256) refine_kernel(GraphView g, const QVert* _
       while (m && __any_sync(kFull, alive)) {
         const uint32_t wv = __ffs(m) - 1;
         const QVert* qw = qv + gbase + wv;
-        uint32_t grp = 0;
-        for (uint32_t r = m; r; r &= r - 1) {
-          const uint32_t x = __ffs(r) - 1;
-          if (qv[gbase + x].cls == qw->cls) grp |= 1u << x;
-        }
+        const uint32_t grp = m & qw->cmask;
         m &= ~grp;
         const uint32_t need = __popc(grp);
         if (alive) {
@@ -461,7 +457,9 @@ struct BatchLayout {
 
 // Bitmap layout of a batch: one bitmap per query vertex over its label's id
 // range, except that members of a refinement class (classes on) use the
-// bitmap of the class's smallest member and own no words.
+// bitmap of the class's smallest member and own no words.  Callers turn
+// classes on only when the refinement runs: without it, sharing saves a few
+// bitmap words of filter output, less than the classes cost on the host.
 void layout_batch(const DeviceGraph& g, const std::vector<HostQuery>& qs, BatchLayout& b, bool classes) {
   b.Q = uint32_t(qs.size());
   b.qoff.assign(size_t(b.Q) + 1, 0);
@@ -491,6 +489,8 @@ void layout_batch(const DeviceGraph& g, const std::vector<HostQuery>& qs, BatchL
       x.u = u;
       x.cls = cls[u];
       x.dom = dom[u];
+      for (uint32_t w = 0; w < h.n; w++)
+        if (cls[w] == cls[u]) x.cmask |= 1u << w;
       std::memcpy(x.sig, h.sig[u], sizeof(x.sig));
       const int32_t l = h.label[u];
       uint32_t lo = 0, hi = 0;
@@ -808,7 +808,7 @@ int run_batch(Engine& e, const std::vector<HostQuery>& qs, const BatchOptions& o
   const DeviceGraph& g = e.g;
   cudaStream_t s = e.stream;
   BatchLayout b;
-  layout_batch(g, qs, b, opt.classes);
+  layout_batch(g, qs, b, opt.classes && opt.refine_iters > 0);
   const uint32_t Q = b.Q;
   out.res.assign(Q, QueryResult());
   out.counts.assign(b.G, 0);
@@ -1230,7 +1230,7 @@ int run_filter_probe(Engine& e, const HostQuery& q, uint32_t filter_mode, int re
   const DeviceGraph& g = e.g;
   std::vector<HostQuery> qs(1, q);
   BatchLayout b;
-  layout_batch(g, qs, b, classes);
+  layout_batch(g, qs, b, classes && refine_iters > 0);
   e.arena.release(g.arena_mark);
   int rc = FSIG_OK;
   QVert* d_qv = upload(e, b.qv, rc);
@@ -1364,6 +1364,7 @@ int run_filter_noalloc(Engine& e, const fsig_query& q, uint32_t filter_mode, uin
     x.deg = uint32_t(__builtin_popcount(adj[u]));
     x.u = u;
     x.cls = uint8_t(u);
+    x.cmask = 1u << u;
     x.dom = uint8_t(kNoClass);
     x.sig[0] = uint32_t(x.label);
     for (uint32_t w = 0; w < n; w++) {

@@ -50,6 +50,7 @@ struct alignas(16) QVert {
   uint32_t u;          // local id
   uint32_t words;      // bitmap words (0: no data vertex carries this label)
   uint32_t bmbase;     // first new id covered by bitmap word 0 (multiple of 32)
+  uint32_t cmask;      // members of its refinement class (local ids)
   uint8_t cls;         // refinement class: local id of its smallest member
   uint8_t dom;         // class whose candidate set contains this class's (kNoClass: none)
   uint8_t alias;       // 1: uses the bitmap of vertex cls (no words of its own)
@@ -97,10 +98,11 @@ struct BatchOptions {
   const float* scores = nullptr;  // host scores per query vertex (kOrderScores), batch order
   bool learned = false;           // score with the loaded order network (kOrderScores)
   uint32_t learned_window = 32;   // positions a vertex may move from the heuristic order (32: any)
-  // Refinement classes (refine_classes): members share one bitmap, a vertex
-  // needs as many data neighbours in a query neighbour class as it has query
-  // neighbours there, and dominated classes are tested first.  Off: every
-  // vertex its own class (per-vertex support, every count one).
+  // Refinement classes (refine_classes), when refine_iters > 0: members
+  // share one bitmap, a vertex needs as many data neighbours in a query
+  // neighbour class as it has query neighbours there, and dominated classes
+  // are tested first.  Off: every vertex its own class (per-vertex support,
+  // every count one).
   bool classes = true;
   // Single-query batches only: write up to emit_cap embeddings to
   // BatchOutput::rows, and enumerate only pass-0 tasks [task_begin, task_end).
