@@ -43,6 +43,35 @@ def test_autotune_finds_the_fastest_setting():
     assert trials[0][0] == autotune.DEFAULTS
 
 
+class WindowEngine(KnobEngine):
+    """Learned order: the window changes device time and which queries go
+    over the work limit (status ELIMIT, no result); heuristic runs cost 3 ms
+    per query."""
+    BATCH_MS = {1: 10.5, 2: 10.2, 4: 10.8, 32: 9.0}
+
+    def match_batch(self, qs, **kw):
+        super().match_batch(qs, **kw)
+        if kw["order_source"] == F.ORDER_HEURISTIC:
+            self.ms = 3.0 * len(qs)
+            return [FakeResult(int(q.labels.size) * 100, 7) for q in qs]
+        w = kw["learned_window"]
+        self.ms += self.BATCH_MS[w] - 10.0
+        over = 2 if w == 32 else 0
+        return [FakeResult(0, 0, F.ELIMIT) if i < over else FakeResult(int(q.labels.size) * 100, 7)
+                for i, q in enumerate(qs)]
+
+
+def test_autotune_learned_window_counts_the_fallback_runs():
+    qs = [query(3 + i) for i in range(4)]
+    best, trials = autotune.tune(WindowEngine(), qs, order_source=F.ORDER_LEARNED, repeats=1)
+    # window 32 is fastest per batch, but its two fallbacks cost 6 ms more
+    assert best["learned_window"] == 2
+    assert best["chunk"] == 2 and best["split_len"] == 512
+    assert trials[0][0] == {**autotune.DEFAULTS, **autotune.LEARNED_DEFAULTS}
+    plain, _ = autotune.tune(KnobEngine(), qs, repeats=1)
+    assert "learned_window" not in plain
+
+
 def test_autotune_rejects_a_setting_that_changes_results():
     with pytest.raises(RuntimeError):
         autotune.tune(KnobEngine(broken=8), [query(3)] * 4, repeats=1)
