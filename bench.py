@@ -13,27 +13,31 @@ compaction + enumeration.
           wall time including packing, host->device copies of the query
           descriptors and device->host copies of the results
 
-Order: the learned order (the packaged order-scoring network,
-fsig_gb300/order_net.npy, trained on logs of the mid-scale graphs) when it
-exists, with a per-query work limit; a query over the limit is carried into
-the next batch with its heuristic order attached (the last ones run in a batch
-of their own), inside the timed region.  After the timed region the same
-batches run in heuristic order ("heuristic_batched"), and every count and
-hash is compared between the two.  "single_query_path" is the plain
-one-query-per-call heuristic path (fsig_match) on a sample.
+Workloads (fsig_gb300/workloads.py): seeded synthetic graphs with the five
+configurations' shapes; the queries of each workload are fixed by its
+manifest (fsig_gb300/manifests/<name>.json), from which both arms rebuild
+them with the host generators.
 
-Workloads (synthetic, seeded; no dataset is available):
-  c5  Chung-Lu 2^22 vertices / 2^26 edges, exponent 2.0, seed 5, 32 Zipf
-      labels; 2048 queries of 12-32 vertices, batches of 512 (default)
-  c4  Chung-Lu 320,000 / 1,050,000, exponent 2.1, seed 2, 16 Zipf labels;
-      4096 queries of 4-32 vertices, half dense half sparse, batches of 512
-  c2  the c4 graph; 200 queries of 8 vertices (100 dense, 100 sparse)
-  c1  R-MAT 10,000 / 50,000, seed 1, 8 uniform labels; 100 queries of 4
+Order: the learned order (the packaged order-scoring network,
+fsig_gb300/order_net.npy) when it exists, with a per-query work limit; a query
+over the limit is carried into the next batch with its heuristic order
+attached (the last ones run in a batch of their own), inside the timed region.
+After the timed region the same batches run in heuristic order
+("heuristic_batched") and every count and hash is compared between the two.
+"single_query_path" is the plain one-query-per-call heuristic path
+(fsig_match) on a sample.  Launch knobs are tuned on the manifest's tuning
+batch, which is never timed.
+
+Parity: cpu_baseline runs the CPU oracle on batch 0's reference subset (the
+queries the CPU arm times) and compares every count and hash with the GPU's
+results for the same queries ("oracle_check"); a mismatch fails the run.
 
 --impl reference times the reference's matching semantics on the host
 cores: the reference's matchers are GPU code with no CPU implementation, so
 this arm runs the CPU backtracking port of them (oracle/) with all host
-threads, each step a bounded sample of the step's batch.
+threads, on each step's reference subset -- the same queries the GPU arm
+reports under "matched_subset".  It loads no library of the engine (its
+generators come from oracle/build.py's copy).
 """
 from __future__ import annotations
 
@@ -54,15 +58,15 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 import fsig_gb300 as F  # noqa: E402
+from fsig_gb300 import workloads as W  # noqa: E402
 
 METRIC = "queries/s & embeddings/s on 1 GB300, learned vs heuristic order, bit-exact"
 PEAKS = ROOT / "MEASURED_PEAKS.json"
 FALLBACK_HBM_GBS = 6800.0
 
-# DRAM bytes per enumeration launch from an ncu capture; None until measured.
-# DRAM bytes (read + write) of one enumerate_kernel launch on a heavy
-# config-5 batch (about 5.4e8 driver windows), from an ncu capture
-# (profiles/enumerate_kernel_c5.md); its loads are served from L2 at 98.9%.
+# DRAM bytes (read + write) of one enumerate_kernel launch on a config-5
+# batch, from an ncu capture (profiles/enumerate_kernel_c5.md); its loads are
+# served from L2 at about 99 %.
 ENUM_TRAFFIC_BYTES_PER_LAUNCH = 286_300_000
 
 
@@ -70,77 +74,21 @@ def log(*a):
     print(*a, file=sys.stderr, flush=True)
 
 
-# ---------------------------------------------------------------------------
-# workloads
-# ---------------------------------------------------------------------------
-def build_graph(name):
-    if name == "c5":
-        lab = F.gen_labels(1 << 22, 32, "zipf", seed=5)
-        return F.gen_chung_lu(1 << 22, 1 << 26, 2.0, seed=5, labels=lab), "Chung-Lu 2^22 V / 2^26 E, exp 2.0, 32 Zipf labels"
-    if name in ("c4", "c2"):
-        lab = F.gen_labels(320000, 16, "zipf", seed=2)
-        return F.gen_chung_lu(320000, 1050000, 2.1, seed=2, labels=lab), "Chung-Lu 320k V / 1.05M E, exp 2.1, 16 Zipf labels"
-    if name == "c1":
-        lab = F.gen_labels(10000, 8, "uniform", seed=1)
-        return F.gen_rmat(10000, 50000, 0.57, 0.19, 0.19, seed=1, labels=lab), "R-MAT 10k V / 50k E, 8 uniform labels"
-    raise SystemExit(f"unknown workload {name}")
+def sig(x: float, digits: int = 6) -> float:
+    """x rounded to `digits` significant digits."""
+    return float(f"{x:.{digits}g}") if x else 0.0
 
 
-# Candidate queries are random-walk extractions in a seeded sequence; a
-# workload keeps, in order, the first ones whose enumeration under the
-# heuristic order examines at most WORK_BUDGET driver entries (a property of
-# query and graph alone, so the choice is the same on every run).  Walks are
-# confined to the less frequent Zipf labels: over all labels, 12-32-vertex
-# queries on the 2^22-vertex graph have more than 10^9 partial embeddings
-# (none of 512 candidates fitted 2^26 examined entries).
-WORK_BUDGET = 1 << 26
-
-
-def candidate_specs(name, rank):
-    rng = np.random.default_rng(1000 + rank)
-    base = 1_000_000 * (rank + 1)
-    if name == "c5":
-        # 2048 dense queries of 12-32 vertices on labels >= 8, batches of 512
-        sizes = rng.integers(12, 33, 32768)
-        return [[(int(n), F.QUERY_DENSE, base + i, 8) for i, n in enumerate(sizes)]], [2048], 512
-    if name == "c4":
-        # 4096 queries of 4-32 vertices, half dense half sparse, labels >= 4
-        sizes = rng.integers(4, 33, 32768)
-        dense = [(int(n), F.QUERY_DENSE, base + i, 4) for i, n in enumerate(sizes)]
-        sparse = [(int(n), F.QUERY_SPARSE, base + 500_000 + i, 4) for i, n in enumerate(sizes)]
-        return [dense, sparse], [2048, 2048], 512
-    if name == "c2":
-        dense = [(8, F.QUERY_DENSE, base + i, 4) for i in range(4096)]
-        sparse = [(8, F.QUERY_SPARSE, base + 500_000 + i, 4) for i in range(4096)]
-        return [dense, sparse], [100, 100], 200
-    if name == "c1":
-        return [[(4, F.QUERY_INDUCED, base + i) for i in range(100)]], [100], 100
-    raise SystemExit(f"unknown workload {name}")
-
-
-def make_workload(name, rank, engine):
-    """Graph (loaded into the engine) and the selected query batches."""
-    t = time.time()
-    g, gdesc = build_graph(name)
-    csr = g.csr()
-    engine.load_graph(g)
-    pools, wants, batch = candidate_specs(name, rank)
-    qs = []
-    for pool, want in zip(pools, wants):
-        picked = []
-        for i in range(0, len(pool), 2048):  # generate candidates in slices, select, stop when enough
-            cand = F.gen_queries(g, pool[i:i + 2048], csr=csr)
-            picked += F.select_within_budget(engine, cand, want - len(picked), WORK_BUDGET)
-            if len(picked) >= want:
-                break
-        if len(picked) < want:
-            raise SystemExit(f"workload {name}: only {len(picked)} of {want} candidates fit the work budget")
-        qs.append(picked)
-    # interleave the pools so that every batch has the same mix
-    mixed = [q for tup in zip(*qs) for q in tup] if len(qs) > 1 else qs[0]
-    batches = [mixed[i:i + batch] for i in range(0, len(mixed), batch)]
-    log(f"[bench] workload {name}: {len(mixed)} queries in {len(batches)} batches, setup {time.time() - t:.1f}s")
-    return g, csr, gdesc, batches
+def shared_config(w: W.Workload, world: int) -> dict:
+    """The workload description both arms print (identical by construction)."""
+    m = w.manifest
+    return {"workload": w.name, "graph": w.desc, "queries_per_step": len(w.batches[0]),
+            "batches": len(w.batches), "manifest": f"fsig_gb300/manifests/{w.name}.json",
+            "selection": f"{m['selection']} ({m['work_budget']})",
+            "reference_subset": m["ref_subset_rule"],
+            "l2": "inputs larger than L2 (resident graph arrays > 129 MB)" if w.name == "c5" else
+                  "graph fits L2; batches differ step to step",
+            "parallelism": f"replicas x{world}, each rank runs the manifest's batches from batch <rank>"}
 
 
 # ---------------------------------------------------------------------------
@@ -247,22 +195,20 @@ def cuda_sync():
 
 
 # ---------------------------------------------------------------------------
-# CPU baseline: the oracle port on the host cores, bounded sample
+# the CPU oracle on a fixed subset of a batch (cpu_baseline, reference arm)
 # ---------------------------------------------------------------------------
-def cpu_sample(g, csr, queries, budget_s):
-    from oracle import oracle as O  # the CPU leg only
-    off, adj = csr
+def oracle_on(w: W.Workload, queries) -> tuple:
+    """(results [(count, hash)], seconds, threads): the oracle's backtracking
+    matcher on the host cores, every query to completion."""
+    from oracle import oracle as O  # the CPU legs only
+    off, adj = w.csr
     threads = os.cpu_count() or 1
     t0 = time.perf_counter()
-    done = emb = 0
+    res = []
     for q in queries:
-        c, h, _ = O.match(g.labels, off, adj, q.labels, q.edges, threads=threads)
-        done += 1
-        emb += c
-        if time.perf_counter() - t0 > budget_s:
-            break
-    dt = time.perf_counter() - t0
-    return done, emb, dt, threads
+        c, h, _ = O.match(w.graph.labels, off, adj, q.labels, q.edges, threads=threads)
+        res.append((int(c), int(h)))
+    return res, time.perf_counter() - t0, threads
 
 
 # ---------------------------------------------------------------------------
@@ -293,13 +239,17 @@ def run_ours(args, dist):
     dev = dist.local
     algo = {"fsig": F.ALGO_FSIG, "gsi": F.ALGO_GSI, "fused": F.ALGO_FUSED}[args.algo]
     order = args.order or ("learned" if learn.WEIGHTS.exists() else "heuristic")
+    t = time.time()
+    w = W.load(args.workload, rank=dist.rank)
+    batches = w.batches
+    log(f"[bench] workload {w.name}: {sum(len(b) for b in batches)} queries in {len(batches)} batches from the "
+        f"manifest, built in {time.time() - t:.1f}s")
     with F.Engine(dev, arena_bytes=args.arena_gb << 30) as e:
-        g, csr, gdesc, batches = make_workload(args.workload, dist.rank, e)
-        info = e.graph_info()
-        log(f"[bench] graph resident: {info}")
+        e.load_graph(w.graph)
+        log(f"[bench] graph resident: {e.graph_info()}")
         if order == "learned":
             e.mpnn_set_params(learn.load_params())
-        limit = args.max_work or (WORK_BUDGET if order == "learned" else 0)
+        limit = args.max_work or (W.WORK_BUDGET if order == "learned" else 0)
 
         use_graph = not args.no_graph
         knobs, tune_note = {}, "defaults"
@@ -307,9 +257,10 @@ def run_ours(args, dist):
             from fsig_gb300 import autotune
             t = time.time()
             osrc = F.ORDER_LEARNED if order == "learned" else F.ORDER_HEURISTIC
-            knobs, trials = autotune.tune(e, batches[-1], algo=algo, order_source=osrc, max_work=limit,
+            knobs, trials = autotune.tune(e, w.tune, algo=algo, order_source=osrc, max_work=limit,
                                           use_graph=use_graph)
-            tune_note = f"coordinate descent on the last batch, {len(trials)} trials, {time.time() - t:.1f}s"
+            tune_note = (f"coordinate descent on the manifest's tuning batch ({len(w.tune)} queries, never timed), "
+                         f"{len(trials)} trials, {time.time() - t:.1f}s")
             log(f"[bench] autotuned {knobs} ({tune_note})")
 
         feed = learn.LearnedFeed(e, algo, limit, use_graph=use_graph, **knobs) if order == "learned" else None
@@ -331,7 +282,7 @@ def run_ours(args, dist):
         dist.barrier()
         cuda_sync()
         acc = StepStats()
-        nq = over = fallbacks = 0
+        nq = fallbacks = 0
         results = [None] * args.steps
         with ClockSampler(dev) as clk:
             t0 = time.perf_counter()
@@ -356,6 +307,9 @@ def run_ours(args, dist):
             wall = time.perf_counter() - t0
         dist.barrier()
         emb = sum(c for step_res in results for c, _ in step_res)
+        # every result against the manifest's record of the same query
+        manifest_equal = all(results[k] == list(zip(w.counts[k % len(batches)], w.hashes[k % len(batches)]))
+                             for k in range(args.steps))
         # the same batches in heuristic order: the comparison and the bit-exactness check
         heur = StepStats()
         identical = True
@@ -378,6 +332,18 @@ def run_ours(args, dist):
             enum_ms, enum_bytes = roof.enum_ms, roof.enum_bytes
             roof_basis = "the timed batches again, launched without a graph"
         launches, h2d, d2h, passes = acc.launches, acc.h2d, acc.d2h, acc.passes
+        # the reference subsets (the queries the CPU arm times), one batch each
+        sub_q = sub_emb = 0
+        sub_dev = sub_wall = 0.0
+        for k in range(len(batches)):
+            qs = [batches[k][i] for i in w.ref_subset[k]]
+            ts = time.perf_counter()
+            rs = e.match_batch(qs, algo=algo, order_source=F.ORDER_HEURISTIC, use_graph=use_graph, **knobs)
+            sub_wall += time.perf_counter() - ts
+            st = e.last_stats()
+            sub_dev += (st["ms_filter"] + st["ms_join"]) / 1e3
+            sub_q += len(qs)
+            sub_emb += sum(r.count for r in rs)
         # the plain single-query path (fsig_match, heuristic order) on a sample
         single = batches[0][: args.single_sample]
         t1 = time.perf_counter()
@@ -399,30 +365,26 @@ def run_ours(args, dist):
     achieved = (enum_bytes / (enum_ms / 1e3)) / 1e9 if enum_ms > 0 else 0.0
     line = {
         "metric": METRIC,
-        "value": round(value, 3),
+        "value": sig(value),
         "unit": "queries/s",
-        "embeddings_per_s": round(tot_emb / dev_s, 1),
+        "embeddings_per_s": sig(tot_emb / dev_s),
         "n_gpus": dist.world,
         "steps": args.steps,
         "warmup": args.warmup,
-        "ms_per_step": round(dev_s * 1e3 / args.steps, 3),
+        "ms_per_step": sig(dev_s * 1e3 / args.steps),
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "u32",
         "data": "synthetic (seeded generators; no dataset available)",
-        "config": {"workload": args.workload, "graph": gdesc, "queries_per_step": len(batches[0]),
-                   "algo": args.algo, "order": order, "parallelism": f"replicas x{dist.world}, queries sharded",
-                   "l2": "inputs larger than L2 (resident graph arrays > 129 MB)" if args.workload in ("c5",) else
-                   "graph fits L2; batches differ step to step",
-                   "work_limit": limit, "cuda_graph": use_graph, "knobs": knobs or "defaults",
-                   "autotune": tune_note, "queries_over_limit": over, "learned_fallbacks": fallbacks,
-                   "selection": f"first queries of a seeded random-walk sequence whose enumeration examines at most "
-                                f"{WORK_BUDGET} driver entries"},
-        "e2e": {"value": round(tot_q / wall_s, 3), "unit": "queries/s",
+        "config": shared_config(w, dist.world),
+        "arm": {"algo": args.algo, "order": order, "work_limit": limit, "cuda_graph": use_graph,
+                "knobs": knobs or "defaults", "autotune": tune_note, "learned_fallbacks": fallbacks,
+                "results_equal_manifest": bool(manifest_equal)},
+        "e2e": {"value": sig(tot_q / wall_s), "unit": "queries/s",
                 "h2d_bytes_per_step": int(h2d / args.steps), "d2h_bytes_per_step": int(d2h / args.steps)},
-        "heuristic_batched": {"value": round(tot_q / heur_s, 3), "unit": "queries/s",
-                              "ms_per_step": round(heur_s * 1e3 / args.steps, 3),
+        "heuristic_batched": {"value": sig(tot_q / heur_s), "unit": "queries/s",
+                              "ms_per_step": sig(heur_s * 1e3 / args.steps),
                               "counts_and_hashes_identical": bool(identical),
                               "note": "the same batches in heuristic order, device time, after the timed region"},
         "latency_ms": {
@@ -432,69 +394,106 @@ def run_ours(args, dist):
             "single_p99": round(1e3 * float(np.percentile(single_lat, 99)), 2),
             "note": "per query, wall clock: a batched query completes with its batch (call to results), a single "
                     "query with its own fsig_match call"},
-        "single_query_path": {"value": round(single_qps, 3), "unit": "queries/s",
+        "single_query_path": {"value": sig(single_qps), "unit": "queries/s",
                               "sample": f"first {len(single)} queries of batch 0, one fsig_match call each (algo 2, "
                                         "reference-exact heuristic order), wall clock"},
+        "matched_subset": {"queries": sub_q, "embeddings": sub_emb,
+                           "gpu_device_qps": sig(sub_q / sub_dev), "gpu_e2e_qps": sig(sub_q / sub_wall),
+                           "gpu_device_emb_per_s": sig(sub_emb / sub_dev),
+                           "note": "each batch's reference subset (the queries the CPU arm times) as one batch, "
+                                   "heuristic order; a few queries per batch, so launch-latency bound"},
         "gpu_launches": int(launches),
         "enumeration_passes": int(passes),
         "roofline": {"bound": "hbm", "kernel": "enumerate_kernel", "achieved": round(achieved, 1),
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
                      "peak_source": "measured" if PEAKS.exists() else "fallback",
                      "traffic": ENUM_TRAFFIC_BYTES_PER_LAUNCH if args.workload == "c5" else None,
-                     "traffic_note": ("DRAM bytes of one heavy config-5 batch launch (ncu); requested bytes are "
-                                      "served from L2 at 98.9% hit: the kernel is issue-bound, not HBM-bound")
+                     "traffic_note": ("DRAM bytes of one config-5 batch launch (ncu); requested bytes are "
+                                      "served from L2 at about 99% hit: the kernel is issue-bound, not HBM-bound")
                                      if args.workload == "c5" else "no ncu capture of this workload",
                      "achieved_basis": "bytes requested by the kernel's global loads / kernel time, "
                                        + roof_basis},
         "clocks": clocks,
     }
     if dist.rank == 0 and not args.no_cpu_baseline:
-        done, cemb, cdt, threads = cpu_sample(g, csr, batches[0], args.cpu_budget)
-        line["cpu_baseline"] = {"value": round(done / cdt, 3), "unit": "queries/s", "cores": threads, "kind": "port",
-                                "sample": f"first {done} queries of batch 0 ({cemb} embeddings), oracle backtracking, "
-                                          f"{threads} threads, {cdt:.1f}s"}
+        sub = w.ref_subset[0]
+        qs = [batches[0][i] for i in sub]
+        ores, cdt, threads = oracle_on(w, qs)
+        gpu = [results[0][i] for i in sub]
+        equal = ores == gpu
+        cemb = sum(c for c, _ in ores)
+        line["cpu_baseline"] = {"value": sig(len(qs) / cdt), "unit": "queries/s", "cores": threads, "kind": "port",
+                                "embeddings_per_s": sig(cemb / cdt),
+                                "sample": f"batch 0's reference subset: {len(qs)} queries ({cemb} embeddings), "
+                                          f"oracle backtracking, {threads} threads, {cdt:.1f}s"}
+        line["oracle_check"] = {"queries": len(qs), "equal": bool(equal),
+                                "note": "oracle (count, hash) against the timed step-0 results of the same queries"}
+        line["matched_subset"]["cpu_qps_batch0"] = sig(len(qs) / cdt)
+        line["matched_subset"]["cpu_emb_per_s_batch0"] = sig(cemb / cdt)
+        if not equal:
+            bad = [i for i, (a, b) in zip(sub, zip(ores, gpu)) if a != b]
+            print(json.dumps(line), flush=True)
+            raise SystemExit(f"oracle check failed on batch 0 queries {bad}")
+    if not identical or not manifest_equal:
+        print(json.dumps(line), flush=True)
+        raise SystemExit("results differ between orders or from the manifest's record")
     return line
 
 
 def run_reference(args, dist):
     if dist.rank != 0:
         return None
-    # The workload's queries are chosen with the GPU engine (a property of
-    # query and graph); the timed work below runs only on the host cores.
-    with F.Engine(dist.local, arena_bytes=args.arena_gb << 30) as e:
-        g, csr, gdesc, batches = make_workload(args.workload, 0, e)
-    per_step = max(1.0, args.ref_step_s)
+    from oracle import build as obuild
+    F.use_generator_library(obuild.build_generators())
+    t = time.time()
+    w = W.load(args.workload)
+    log(f"[reference] workload {w.name} built in {time.time() - t:.1f}s (generators from oracle/_build)")
+    nb = len(w.batches)
+    # warm-up: the first query of each step's subset
     for i in range(args.warmup):
-        cpu_sample(g, csr, batches[i % len(batches)], per_step / 4)
-    done_tot = emb_tot = 0
-    t0 = time.perf_counter()
+        k = i % nb
+        oracle_on(w, [w.batches[k][j] for j in w.ref_subset[k][:1]])
+    done = emb = 0
+    checked = mismatched = 0
     threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    step_s = []
     for k in range(args.steps):
-        done, emb, dt, threads = cpu_sample(g, csr, batches[k % len(batches)], per_step)
-        done_tot += done
-        emb_tot += emb
+        b = k % nb
+        idx = w.ref_subset[b]
+        res, dt, threads = oracle_on(w, [w.batches[b][j] for j in idx])
+        step_s.append(dt)
+        done += len(idx)
+        emb += sum(c for c, _ in res)
+        for j, r in zip(idx, res):
+            checked += 1
+            mismatched += r != (w.counts[b][j], w.hashes[b][j])
+        log(f"[reference] step {k}: {len(idx)} queries of batch {b}, {dt:.2f}s")
     dt = time.perf_counter() - t0
-    v = done_tot / dt
-    sample = (f"per step: the first queries of the step's batch until {per_step:.0f}s, oracle backtracking "
-              f"(the reference's matchers exist only as GPU code), {threads} threads")
+    v = done / dt
+    sample = (f"per step, the step's batch's reference subset ({min(len(s) for s in w.ref_subset)}-"
+              f"{max(len(s) for s in w.ref_subset)} queries; the GPU arm's 'matched_subset' times the same "
+              f"queries), oracle backtracking (the reference's matchers exist only as GPU code), {threads} threads")
     return {
         "impl": "reference",
         "metric": METRIC,
-        "value": round(v, 3),
+        "value": sig(v),
         "unit": "queries/s",
-        "embeddings_per_s": round(emb_tot / dt, 1),
+        "embeddings_per_s": sig(emb / dt),
         "n_gpus": dist.world,
         "steps": args.steps,
         "warmup": args.warmup,
-        "ms_per_step": round(dt * 1e3 / args.steps, 3),
+        "ms_per_step": sig(dt * 1e3 / args.steps),
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "u32",
         "data": "synthetic (seeded generators; no dataset available)",
-        "config": {"workload": args.workload, "graph": gdesc, "queries_per_step": len(batches[0])},
-        "cpu_baseline": {"value": round(v, 3), "unit": "queries/s", "cores": threads, "kind": "port", "sample": sample},
-        "e2e": {"value": round(v, 3), "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "config": shared_config(w, dist.world),
+        "cpu_baseline": {"value": sig(v), "unit": "queries/s", "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": sig(v), "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "oracle_vs_manifest": {"queries": checked, "mismatched": mismatched,
+                               "note": "oracle (count, hash) against the engine's results recorded in the manifest"},
     }
 
 
@@ -511,8 +510,6 @@ def main():
     ap.add_argument("--max-work", type=int, default=0,
                     help="per-query work limit (default: the selection budget in learned order, none otherwise)")
     ap.add_argument("--arena-gb", type=int, default=64)
-    ap.add_argument("--cpu-budget", type=float, default=15.0)
-    ap.add_argument("--ref-step-s", type=float, default=8.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-graph", action="store_true", help="ordinary launches instead of one CUDA graph per batch")
     ap.add_argument("--no-autotune", action="store_true", help="default launch knobs instead of autotuned ones")

@@ -56,7 +56,7 @@ class _BatchOpts(C.Structure):
     _fields_ = [("algo", C.c_int), ("order_source", C.c_int), ("refine_iters", C.c_int), ("use_graph", C.c_int),
                 ("chunk", C.c_uint32), ("split_len", C.c_uint32), ("split_cycles", C.c_uint64),
                 ("max_work", C.c_uint64), ("warps_per_block", C.c_uint32), ("learned_window", C.c_uint32),
-                ("no_classes", C.c_uint32)]
+                ("no_classes", C.c_uint32), ("isect", C.c_uint32), ("refine_coop", C.c_uint32)]
 
 
 class _Stats(C.Structure):
@@ -126,6 +126,9 @@ def engine_library() -> C.CDLL:
                                   C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
     L.fsig_last_stats.argtypes = [vp, C.POINTER(_Stats)]
     L.fsig_filter_noalloc.argtypes = [vp, C.POINTER(_Query), C.c_int, C.c_void_p]
+    L.fsig_set_queue_waits.argtypes = [vp, C.c_uint64, C.c_uint64, C.c_int]
+    L.fsig_match_range.argtypes = [vp, C.POINTER(_Query), C.c_int, C.c_uint32, C.c_uint32, C.c_uint32,
+                                   C.POINTER(_Result), C.POINTER(C.c_uint32)]
     fp = C.POINTER(C.c_float)
     L.fsig_mpnn_param_count.restype = C.c_uint32
     L.fsig_mpnn_param_count.argtypes = []
@@ -147,7 +150,7 @@ def engine_library() -> C.CDLL:
     L.fsig_write_embeddings.argtypes = [vp, C.POINTER(_Query), C.c_int, C.c_char_p, C.POINTER(_Result)]
     for name in ("fsig_mpnn_set_params", "fsig_mpnn_get_params", "fsig_mpnn_features", "fsig_mpnn_forward",
                  "fsig_mpnn_train_step", "fsig_read_graph_file", "fsig_read_graph_file_threads", "fsig_save_graph_cache", "fsig_load_graph_cache", "fsig_graph_file_data", "fsig_match_embeddings",
-                 "fsig_write_embeddings", "fsig_build_pcsr", "fsig_filter_noalloc", "fsig_last_stats", "fsig_plan_order", "fsig_create", "fsig_destroy", "fsig_load_graph", "fsig_load_graph_file", "fsig_graph_info",
+                 "fsig_write_embeddings", "fsig_build_pcsr", "fsig_filter_noalloc", "fsig_set_queue_waits", "fsig_match_range", "fsig_last_stats", "fsig_plan_order", "fsig_create", "fsig_destroy", "fsig_load_graph", "fsig_load_graph_file", "fsig_graph_info",
                  "fsig_match", "fsig_match_batch", "fsig_build_csr", "fsig_build_signature", "fsig_filter",
                  "fsig_filter_classes", "fsig_refine_classes"):
         getattr(L, name).restype = C.c_int
@@ -155,14 +158,28 @@ def engine_library() -> C.CDLL:
     return L
 
 
+_gen_path = None
+
+
+def use_generator_library(path) -> None:
+    """Binds the workload generators to another build of csrc/gen.cpp (the
+    CPU benchmark arm uses the copy oracle/build.py makes, so that it loads
+    none of this package's libraries).  Call before the first generator."""
+    global _gen, _gen_path
+    if _gen is not None and Path(path) != _gen_path:
+        raise RuntimeError("the generator library is already loaded")
+    _gen_path = Path(path)
+
+
 def gen_library() -> C.CDLL:
-    global _gen
+    global _gen, _gen_path
     if _gen is not None:
         return _gen
-    path = _BUILD / "libfsig_gen.so"
-    if not path.exists():
+    path = _gen_path or _BUILD / "libfsig_gen.so"
+    if _gen_path is None and not path.exists():
         from . import _build
         _build.build_gen()
+    _gen_path = path
     L = C.CDLL(str(path))
     L.fsig_gen_rmat.argtypes = [C.c_uint32, C.c_uint64, C.c_double, C.c_double, C.c_double, C.c_uint64, C.c_int,
                                 C.POINTER(C.c_uint32)]
@@ -392,6 +409,11 @@ def _pack_queries(qs: Sequence[Query]):
     labels, edges and orders of all queries in three arrays, the structs as one
     structured array pointing into them.  Returns (pointer, arrays to keep)."""
     n = len(qs)
+    for i, q in enumerate(qs):
+        # each order pointer is placed by its query's vertex count
+        if q.order is not None and np.asarray(q.order).size != np.asarray(q.labels).size:
+            raise ValueError(f"query {i}: an order of {np.asarray(q.order).size} vertices for "
+                             f"{np.asarray(q.labels).size} query vertices")
     labs = [np.asarray(q.labels, np.int32).reshape(-1) for q in qs]
     eds = [np.asarray(q.edges, np.uint32).reshape(-1) for q in qs]
     ords = [np.asarray(q.order, np.uint32).reshape(-1) for q in qs if q.order is not None]
@@ -488,13 +510,33 @@ class Engine:
     def match_batch(self, qs: Sequence[Query], algo: int = ALGO_FUSED, order_source: int = ORDER_HEURISTIC,
                     refine_iters: int = -1, chunk: int = 0, use_graph: bool = False, split_len: int = 0,
                     split_cycles: int = 0, max_work: int = 0, warps_per_block: int = 0,
-                    learned_window: int = 0, classes: bool = True) -> list:
+                    learned_window: int = 0, classes: bool = True, isect: int = 0, refine_coop: int = 0) -> list:
         arr, keep = _pack_queries(qs)
         res = (_Result * max(len(qs), 1))()
         opts = _BatchOpts(algo, order_source, refine_iters, 1 if use_graph else 0, chunk, split_len, split_cycles,
-                          max_work, warps_per_block, learned_window, 0 if classes else 1)
+                          max_work, warps_per_block, learned_window, 0 if classes else 1, isect, refine_coop)
         self._check(self._L.fsig_match_batch(self._h, len(qs), arr, C.byref(opts), res), "match_batch")
         return [_result(res[i]) for i in range(len(qs))]
+
+    def set_queue_waits(self, ready_wait_ns: int = 0, idle_wait_ns: int = 0, unpublished: bool = False) -> None:
+        """Bounded waits of the enumeration's work queue (0: defaults, 200 ms
+        and 2 s); unpublished=True leaves each pass's first handed-off record
+        unpublished (fault injection for tests: the call returns ETIMEOUT)."""
+        self._check(self._L.fsig_set_queue_waits(self._h, int(ready_wait_ns), int(idle_wait_ns), int(unpublished)),
+                    "set_queue_waits")
+
+    def match_range(self, q: Query, algo: int = ALGO_FSIG, task_begin: int = 0, task_end: int = 0xFFFFFFFF,
+                    split_len: int = 0):
+        """Count and hash of the query over root tasks [task_begin, task_end);
+        returns (Result, size of the task space).  Ranges that partition the
+        space add up to the whole query's result (hashes modulo 2^64)."""
+        keep = []
+        cq = _as_cquery(q, keep)
+        r = _Result()
+        T = C.c_uint32()
+        self._check(self._L.fsig_match_range(self._h, C.byref(cq), algo, split_len, task_begin, task_end, C.byref(r),
+                                             C.byref(T)), "match_range")
+        return _result(r), int(T.value)
 
     def last_stats(self) -> dict:
         st = _Stats()

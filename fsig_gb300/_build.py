@@ -26,6 +26,9 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-Xptxas", "-warn-spills"]
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-Wall", "-Wno-unused-function"]
+# The generators must give the same graphs on x86-64 and AArch64: no fused
+# multiply-add contraction (GCC contracts by default on AArch64).
+GEN_FLAGS = ["-ffp-contract=off"]
 
 ENGINE_SOURCES = ["graph_store.cu", "match.cu", "capi.cu", "mpnn.cu", "pcsr.cu", "plan.cu", "reader.cpp"]
 GEN_SOURCES = ["gen.cpp"]
@@ -84,7 +87,8 @@ def build_gen(force: bool = False) -> Path:
     lib = OUT / "libfsig_gen.so"
     sources = [CSRC / s for s in GEN_SOURCES]
     if force or _stale(lib, [*sources, INCLUDE / "fsig_gen.h"]):
-        _run(["g++", *CXX_FLAGS, "-shared", "-pthread", "-I", str(INCLUDE), "-o", str(lib), *map(str, sources)])
+        _run(["g++", *CXX_FLAGS, *GEN_FLAGS, "-shared", "-pthread", "-I", str(INCLUDE), "-o", str(lib),
+              *map(str, sources)])
     return lib
 
 

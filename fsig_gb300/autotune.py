@@ -1,6 +1,6 @@
 """Autotuner of the batched path's launch knobs, by measurement.
 
-The enumeration kernel's behaviour on a workload depends on four knobs of
+The enumeration kernel's behaviour on a workload depends on five knobs of
 ``fsig_batch_opts``:
 
 * ``warps_per_block`` - block size of the persistent enumeration launch
@@ -9,13 +9,21 @@ The enumeration kernel's behaviour on a workload depends on four knobs of
 * ``split_len`` - driver entries per task range (the unit of root tasks and
   hand-offs, and so of load balance);
 * ``split_cycles`` - SM cycles a task runs before its unexplored frontier may
-  be handed to idle warps.
+  be handed to idle warps;
+* ``isect`` - the set-intersection strategy of the membership tests: 0
+  adaptive (the 32 entries after a segment's cursor first, merge-like, then a
+  warp-cooperative 32-ary window search, shuffle search of windows of <= 32
+  entries and per-lane binary search of longer ones), 1 window search only
+  (galloping-like), 2 per-lane binary search of the whole segment.
 
-The set-intersection strategy needs no knob: the kernel picks per driver
-window between the warp-cooperative 32-ary window search and per-lane binary
-search from the list-length ratio.
+When the batch refines candidates (``refine_iters`` > 0) one more joins:
 
-With ``order_source = ORDER_LEARNED`` a fifth knob joins the grid:
+* ``refine_coop`` - warps per candidate in the refinement: a candidate whose
+  neighbour segment is longer than this is scanned by the whole warp
+  (coalesced, one ballot per 32 entries), shorter ones by the candidate's own
+  lane.
+
+With ``order_source = ORDER_LEARNED`` another knob joins the grid:
 
 * ``learned_window`` - positions a vertex may move away from the heuristic
   order.  It changes the orders and with them the work; a query whose learned
@@ -40,8 +48,11 @@ GRID = {
     "chunk": [1, 2, 4, 8],
     "split_len": [64, 128, 256, 512, 1024],
     "split_cycles": [1000, 4000, 16000, 64000],
+    "isect": [0, 1, 2],
 }
-DEFAULTS = {"warps_per_block": 8, "chunk": 1, "split_len": 256, "split_cycles": 4000}
+DEFAULTS = {"warps_per_block": 8, "chunk": 1, "split_len": 256, "split_cycles": 4000, "isect": 0}
+REFINE_GRID = {"refine_coop": [8, 32, 128, 0xFFFFFFFF]}
+REFINE_DEFAULTS = {"refine_coop": 32}
 LEARNED_GRID = {"learned_window": [1, 2, 4, 32]}
 LEARNED_DEFAULTS = {"learned_window": 32}
 
@@ -76,8 +87,9 @@ def tune(engine: Engine, batch: Sequence[Query], algo: int = ALGO_FUSED, order_s
     `fixed` (e.g. max_work, use_graph) is passed to every run unchanged."""
     base = dict(algo=algo, order_source=order_source, **fixed)
     learned = order_source == ORDER_LEARNED
-    grid = {**GRID, **LEARNED_GRID} if learned else GRID
-    best = {**DEFAULTS, **LEARNED_DEFAULTS} if learned else dict(DEFAULTS)
+    refines = fixed.get("refine_iters", -1) > 0 or (algo == 1 and fixed.get("refine_iters", -1) != 0)
+    grid = {**GRID, **(LEARNED_GRID if learned else {}), **(REFINE_GRID if refines else {})}
+    best = {**DEFAULTS, **(LEARNED_DEFAULTS if learned else {}), **(REFINE_DEFAULTS if refines else {})}
     engine.match_batch(batch, **base, **best)  # warm-up
     best_ms, want = _time(engine, batch, {**base, **best}, repeats, None)
     trials = [(dict(best), best_ms)]

@@ -251,6 +251,34 @@ int fsig_match(fsig_engine* h, const fsig_query* q, int algo, fsig_result* out) 
   return FSIG_OK;
 }
 
+int fsig_match_range(fsig_engine* h, const fsig_query* q, int algo, uint32_t split_len, uint32_t task_begin,
+                     uint32_t task_end, fsig_result* out, uint32_t* tasks_total) {
+  int rc = select(h);
+  if (rc) return finish(h, rc);
+  if (!q || !out) return finish(h, fsig::fail(FSIG_EINVAL, "null argument"));
+  if (algo != FSIG_ALGO_FSIG && algo != FSIG_ALGO_GSI && algo != FSIG_ALGO_FUSED)
+    return finish(h, fsig::fail(FSIG_EINVAL, "unknown algorithm"));
+  if (task_begin > task_end) return finish(h, fsig::fail(FSIG_EINVAL, "task_begin > task_end"));
+  std::memset(out, 0, sizeof(*out));
+  std::vector<fsig::HostQuery> qs(1);
+  rc = fsig::prepare_query(*q, h->e.has_graph ? h->e.g.L : 0, qs[0]);
+  if (rc) { out->status = rc; return finish(h, rc); }
+  fsig::BatchOptions o;
+  algo_options(algo, -1, o);
+  if (!qs[0].has_given) o.host_order = algo == FSIG_ALGO_FSIG ? fsig::mmatch_order_host : fsig::gsi_order_host;
+  else o.order_mode = fsig::kOrderGiven;
+  o.split = split_len ? std::max<uint32_t>(split_len, 32u) : 256u;
+  o.task_begin = task_begin;
+  o.task_end = task_end;
+  o.want_tasks = true;
+  fsig::BatchOutput bo;
+  rc = fsig::run_batch(h->e, qs, o, bo);
+  if (rc) { out->status = rc; return finish(h, rc); }
+  fill_result(qs[0], bo, 0, 0, out);
+  if (tasks_total) *tasks_total = bo.tasks_total;
+  return FSIG_OK;
+}
+
 int fsig_read_graph_file(const char* path, int is_labeled, fsig_graph_file** out) {
   return fsig_read_graph_file_threads(path, is_labeled, 0, out);
 }
@@ -352,7 +380,7 @@ int fsig_match_batch(fsig_engine* h, uint32_t nq, const fsig_query* qs, const fs
   int rc = select(h);
   if (rc) return finish(h, rc);
   if ((nq && (!qs || !out))) return finish(h, fsig::fail(FSIG_EINVAL, "null argument"));
-  fsig_batch_opts def{FSIG_ALGO_FUSED, FSIG_ORDER_HEURISTIC, -1, 0, 0, 0, 0, 0, 0, 0, 0};
+  fsig_batch_opts def{FSIG_ALGO_FUSED, FSIG_ORDER_HEURISTIC, -1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   const fsig_batch_opts& bo = opts ? *opts : def;
   if (bo.algo != FSIG_ALGO_FSIG && bo.algo != FSIG_ALGO_GSI && bo.algo != FSIG_ALGO_FUSED)
     return finish(h, fsig::fail(FSIG_EINVAL, "unknown algorithm"));
@@ -386,6 +414,9 @@ int fsig_match_batch(fsig_engine* h, uint32_t nq, const fsig_query* qs, const fs
   if (bo.split_len) o.split = bo.split_len;
   if (bo.split_cycles) o.budget_cycles = (long long)bo.split_cycles;
   o.max_work = bo.max_work;
+  if (bo.isect > 2) return finish(h, fsig::fail(FSIG_EINVAL, "unknown intersection strategy"));
+  o.isect = bo.isect;
+  if (bo.refine_coop) o.refine_coop = bo.refine_coop;
   fsig::BatchOutput out_b;
   rc = fsig::run_batch(h->e, hq, o, out_b);
   if (rc) return finish(h, rc);
@@ -447,6 +478,17 @@ int fsig_mpnn_train_step(fsig_engine* h, uint32_t ng, const uint32_t* goff, cons
 int fsig_last_stats(const fsig_engine* h, fsig_batch_stats* out) {
   if (!h || !out) return FSIG_EINVAL;
   *out = h->e.last;
+  return FSIG_OK;
+}
+
+int fsig_set_queue_waits(fsig_engine* h, uint64_t ready_wait_ns, uint64_t idle_wait_ns, int unpublished) {
+  if (!h) return FSIG_EINVAL;
+  constexpr uint64_t kMaxWaitNs = 60ull * 1000000000ull;
+  if (ready_wait_ns > kMaxWaitNs || idle_wait_ns > kMaxWaitNs || (unpublished != 0 && unpublished != 1))
+    return FSIG_EINVAL;
+  h->e.ready_wait_ns = ready_wait_ns ? ready_wait_ns : 200000000ull;
+  h->e.idle_wait_ns = idle_wait_ns ? idle_wait_ns : 2000000000ull;
+  h->e.inject_unpublished = uint32_t(unpublished);
   return FSIG_OK;
 }
 

@@ -10,6 +10,8 @@
 
 namespace fsig {
 
+constexpr uint32_t kMaxLabels = 4096;  // labels 0..4095 in a loaded data graph
+
 // The resident data graph, renumbered so that every label class occupies a
 // contiguous id range: new ids are sorted by (label, caller id).  In this id
 // space a row of the adjacency sorted by id is also sorted by neighbour
@@ -57,6 +59,10 @@ struct Engine {
   struct MpnnState* mpnn = nullptr;      // order-scoring network (mpnn.cu), created on first use
   bool mpnn_configured = false;          // its kernels' shared-memory attributes are set
   cudaGraphExec_t gexec = nullptr;       // the last batch's executable graph, updated in place
+  // bounded waits of the enumeration's work queue (fsig_set_queue_waits)
+  uint64_t ready_wait_ns = 200000000ull;   // a taken record's publication: 200 ms
+  uint64_t idle_wait_ns = 2000000000ull;   // an idle warp waiting for hand-offs: 2 s
+  uint32_t inject_unpublished = 0;         // test hook: leave each pass's first hand-off unpublished
 };
 
 // graph_store.cu

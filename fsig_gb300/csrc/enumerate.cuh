@@ -75,13 +75,33 @@ struct EnumArgs {
   uint32_t* emit;
   unsigned long long emit_cap;
   unsigned long long* emit_ctr;
+  // bounded waits (nanoseconds of the GPU's global timer): how long a warp
+  // waits for a record it took to be published, and how long an idle warp
+  // waits for hand-offs before it leaves (its queued work runs in a later pass)
+  unsigned long long ready_wait_ns;
+  unsigned long long idle_wait_ns;
+  // fault injection for tests: the first record handed off in the pass is
+  // written but never published, so the warp that takes it waits out
+  // ready_wait_ns and the pass reports a timeout
+  uint32_t unpublished;
+  // set-intersection strategy (kIsect*)
+  uint32_t isect;
 };
+
+// Membership of a window's entries in a backward segment:
+constexpr uint32_t kIsectAdaptive = 0;  // the 32 entries after the cursor first (merge-like), else window search
+constexpr uint32_t kIsectSearch = 1;    // 32-ary window search from the cursor (galloping-like)
+constexpr uint32_t kIsectBinary = 2;    // every lane binary-searches the rest of the segment alone
 
 constexpr uint32_t kErrTimeout = 1u;
 constexpr uint32_t kCtrStride = 32;        // one 128-byte line per counter
 constexpr uint32_t kMaxWaiters = 2048;     // warps beyond this many idle ones leave instead of waiting
-constexpr uint32_t kReadySpinLimit = 1u << 22;
-constexpr uint32_t kIdleSpinLimit = 1u << 22;
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
 
 struct WarpSmem {
   Plan plan;
@@ -138,8 +158,9 @@ __global__ void __launch_bounds__(kEnumWarps * 32, kEnumMinBlocks) enumerate_ker
   uint32_t f = 0, dpos = 0, dend = 0, drv = 0, cnt = 0, it = 0;
   unsigned long long S = 0, lc = 0;
   unsigned long long my_count = 0, my_hash = 0, bytes = 0;
-  unsigned long long pend = 0;  // driver entries examined, not yet published to res.work (lane 0)
-  unsigned long long n_tasks = 0, n_pops = 0, n_handoffs = 0, n_recs = 0, n_examine = 0;  // lane 0
+  uint32_t pend = 0;  // driver entries examined, not yet published to res.work (lane 0; flushed every 64 windows)
+  // event counters (lane 0); a warp's share of one launch fits 32 bits
+  uint32_t n_tasks = 0, n_pops = 0, n_handoffs = 0, n_recs = 0, n_examine = 0;
   uint32_t cur_q = kInvalid;
 
   auto flush = [&]() {
@@ -164,7 +185,7 @@ __global__ void __launch_bounds__(kEnumWarps * 32, kEnumMinBlocks) enumerate_ker
     int stop = 0;
     if (lane == 0) {
       if (pend) {
-        const unsigned long long tot = atomicAdd(&A.res[cur_q].work, pend) + pend;
+        const unsigned long long tot = atomicAdd(&A.res[cur_q].work, (unsigned long long)pend) + pend;
         pend = 0;
         if (tot > A.work_cap) atomicExch(&A.res[cur_q].aborted, 1u);
       }
@@ -216,93 +237,65 @@ __global__ void __launch_bounds__(kEnumWarps * 32, kEnumMinBlocks) enumerate_ker
     }
   };
 
-  // Examines the next 32 driver entries of depth lv.  x: candidate (new id);
-  // xo (leaf only): its caller id.  At the leaf depth the driver windows are
-  // examined in ascending order without leaving the depth, so lane j keeps in
-  // cur the position in backward segment j below which no later window's
-  // entries can lie (the end of the last window found there), and searches
-  // from it, first within the 32 entries that follow it.
-  auto examine = [&](uint32_t lv, bool leaf, uint32_t& x, uint32_t& xo, uint32_t& cur) -> bool {
-    const uint32_t dp = __shfl_sync(kFull, dpos, lv), de = __shfl_sync(kFull, dend, lv);
-    const uint32_t dv = __shfl_sync(kFull, drv, lv);
-    const int32_t lab = ws.plan.lab[lv];
-    uint32_t bw = ws.plan.bwd[lv] & ~(1u << dv);
-    uint32_t my_lo = 0, my_hi = 0;
-    if ((bw >> lane) & 1u) {
-      const uint32_t* s = g.lseg + uint64_t(f) * W1 + lab;
-      my_lo = s[0];
-      my_hi = s[1];
-      bytes += 8;
-    }
-    const uint32_t nvalid = min(32u, de - dp);
-    const uint32_t k = dp + lane;
-    bool pred = lane < nvalid;
-    x = pred ? __ldg(g.adj + k) : 0xffffffffu;
-    xo = (pred && leaf) ? __ldg(g.adj_old + k) : 0u;
-    if (pred) bytes += leaf ? 8 : 4;
-    if (pred) {
-      const uint32_t bit = x - ws.plan.bmbase[lv];
-      const uint32_t bmw = __ldg(A.pool + ws.plan.bmoff[lv] + (bit >> 5));
-      bytes += 4;
-      pred = (bmw >> (bit & 31)) & 1u;
-    }
-    uint32_t sm = ws.plan.same[lv];
-    while (sm) {
-      const uint32_t j = __ffs(sm) - 1;
-      sm &= sm - 1;
-      const uint32_t fj = __shfl_sync(kFull, f, j);
-      pred = pred && x != fj;
-    }
+  // Membership of the window's surviving entries (x, lanes in pred) in every
+  // backward segment of bw, lane j holding segment j as [seg_lo, seg_hi).
+  // Windows of one scan are examined in ascending order, so seg_lo doubles as
+  // a cursor: no later window's entries lie below the end of the last window
+  // found there.  The 32 entries after the cursor are loaded first; when the
+  // window lies among them it is searched there by shuffles (merge-like),
+  // otherwise found by 32-ary searches and searched by shuffles (<= 32
+  // entries) or per-lane binary search (galloping-like).
+  auto member = [&](uint32_t bw, uint32_t x, bool pred, uint32_t& seg_lo, uint32_t seg_hi) -> bool {
     const uint32_t alive = __ballot_sync(kFull, pred);
-    if (bw && alive) {
-      const uint32_t xfirst = __shfl_sync(kFull, x, __ffs(alive) - 1);
-      const uint32_t xlast = __shfl_sync(kFull, x, 31 - __clz(alive));
-      if (leaf) my_lo = max(my_lo, cur);
-      while (bw) {
-        const uint32_t j = __ffs(bw) - 1;
-        bw &= bw - 1;
-        const uint32_t lo = __shfl_sync(kFull, my_lo, j), hi = __shfl_sync(kFull, my_hi, j);
-        uint32_t a, b;
-        bool have = false;
-        if (leaf) {
-          // the 32 entries after the cursor hold the window when it is near
-          const uint32_t idx = lo + lane;
-          const uint32_t v = idx < hi ? __ldg(g.adj + idx) : 0xffffffffu;
-          if (idx < hi) bytes += 4;
-          const uint32_t ta = __popc(__ballot_sync(kFull, v < xfirst));
-          const uint32_t tb = __popc(__ballot_sync(kFull, v <= xlast));
-          const bool ends = lo + 32 >= hi;
-          if (tb < 32 || ends) {
-            // window [lo + ta, lo + tb) lies in this tile: shuffle search
-            a = lo + ta;
-            b = lo + tb;
-            uint32_t l2 = ta, h2 = tb;
+    if (!bw || !alive) return pred;
+    const uint32_t xfirst = __shfl_sync(kFull, x, __ffs(alive) - 1);
+    const uint32_t xlast = __shfl_sync(kFull, x, 31 - __clz(alive));
+    while (bw) {
+      const uint32_t j = __ffs(bw) - 1;
+      bw &= bw - 1;
+      const uint32_t lo = __shfl_sync(kFull, seg_lo, j), hi = __shfl_sync(kFull, seg_hi, j);
+      if (A.isect == kIsectBinary) {
+        // no cooperation and no cursor: each surviving lane searches alone
+        if (pred) pred = bsearch_range(g.adj, lo, hi, x, bytes);
+        if (__ballot_sync(kFull, pred) == 0) break;
+        continue;
+      }
+      uint32_t v = 0xffffffffu, ta = 0, tb = 32;
+      if (A.isect == kIsectAdaptive) {
+        const uint32_t idx = lo + lane;
+        v = idx < hi ? __ldg(g.adj + idx) : 0xffffffffu;
+        if (idx < hi) bytes += 4;
+        ta = __popc(__ballot_sync(kFull, v < xfirst));
+        tb = __popc(__ballot_sync(kFull, v <= xlast));
+      }
+      uint32_t a, b;
+      if (A.isect == kIsectAdaptive && (tb < 32 || lo + 32 >= hi)) {
+        // window [lo + ta, lo + tb) lies in this tile: shuffle search
+        b = lo + tb;
+        uint32_t l2 = ta, h2 = tb;
 #pragma unroll
-            for (int step = 0; step < 6; step++) {
-              const uint32_t mid = (l2 + h2) >> 1;
-              const uint32_t y = __shfl_sync(kFull, v, mid & 31);
-              if (l2 < h2) {
-                if (y < x) l2 = mid + 1; else h2 = mid;
-              }
-            }
-            const uint32_t y = __shfl_sync(kFull, v, l2 & 31);
-            pred = pred && l2 < tb && y == x;
-            have = true;
-          } else if (ta < 32) {
-            a = lo + ta;
-            b = warp_lower_bound(g.adj, lo + 32, hi, xlast + 1, lane, bytes);
-          } else {
-            a = warp_lower_bound(g.adj, lo + 32, hi, xfirst, lane, bytes);
-            b = warp_lower_bound(g.adj, a, hi, xlast + 1, lane, bytes);
+        for (int step = 0; step < 6; step++) {
+          const uint32_t mid = (l2 + h2) >> 1;
+          const uint32_t y = __shfl_sync(kFull, v, mid & 31);
+          if (l2 < h2) {
+            if (y < x) l2 = mid + 1; else h2 = mid;
           }
-          if (lane == j) cur = b;
-        } else {
+        }
+        const uint32_t y = __shfl_sync(kFull, v, l2 & 31);
+        pred = pred && l2 < tb && y == x;
+      } else {
+        if (A.isect == kIsectSearch) {
           a = warp_lower_bound(g.adj, lo, hi, xfirst, lane, bytes);
+          b = warp_lower_bound(g.adj, a, hi, xlast + 1, lane, bytes);
+        } else if (ta < 32) {
+          a = lo + ta;
+          b = warp_lower_bound(g.adj, lo + 32, hi, xlast + 1, lane, bytes);
+        } else {
+          a = warp_lower_bound(g.adj, lo + 32, hi, xfirst, lane, bytes);
           b = warp_lower_bound(g.adj, a, hi, xlast + 1, lane, bytes);
         }
         const uint32_t w = b - a;
-        if (have) {
-        } else if (w == 0) {
+        if (w == 0) {
           pred = false;
         } else if (w <= 32) {
           const uint32_t tile = lane < w ? __ldg(g.adj + a + lane) : 0xffffffffu;
@@ -311,23 +304,19 @@ __global__ void __launch_bounds__(kEnumWarps * 32, kEnumMinBlocks) enumerate_ker
 #pragma unroll
           for (int step = 0; step < 6; step++) {
             const uint32_t mid = (l2 + h2) >> 1;
-            const uint32_t v = __shfl_sync(kFull, tile, mid & 31);
+            const uint32_t y = __shfl_sync(kFull, tile, mid & 31);
             if (l2 < h2) {
-              if (v < x) l2 = mid + 1; else h2 = mid;
+              if (y < x) l2 = mid + 1; else h2 = mid;
             }
           }
-          const uint32_t v = __shfl_sync(kFull, tile, l2 & 31);
-          pred = pred && l2 < w && v == x;
+          const uint32_t y = __shfl_sync(kFull, tile, l2 & 31);
+          pred = pred && l2 < w && y == x;
         } else if (pred) {
           pred = bsearch_range(g.adj, a, b, x, bytes);
         }
-        if (__ballot_sync(kFull, pred) == 0) break;
       }
-    }
-    if (lane == lv) dpos = dp + kChunk;
-    if (lane == 0) {
-      n_examine++;
-      pend += nvalid;
+      if (lane == j) seg_lo = b;
+      if (__ballot_sync(kFull, pred) == 0) break;
     }
     return pred;
   };
@@ -382,20 +371,24 @@ __global__ void __launch_bounds__(kEnumWarps * 32, kEnumMinBlocks) enumerate_ker
     }
     __threadfence();
     __syncwarp();
-    for (uint32_t s = base + lane; s < base + total; s += 32) atomicExch(&A.out_ready[s], A.tag);
+    int hold = 0;  // test hook: keep the pass's first handed-off record unpublished
+    if (A.unpublished && lane == 0) hold = atomicCAS(&A.ctr[6 * kCtrStride], 0u, 1u) == 0u;
+    hold = __shfl_sync(kFull, hold, 0);
+    for (uint32_t s = base + lane; s < base + total; s += 32)
+      if (!(hold && s == base)) atomicExch(&A.out_ready[s], A.tag);
     if (lane == 0) { n_handoffs++; n_recs += total; }
     return true;
   };
 
   // Whether idle warps are waiting for more work than the queue holds.
   // Decided by lane 0 alone and broadcast.
-  auto should_split = [&](long long t_start) -> bool {
+  auto should_split = [&](uint32_t t_start) -> bool {
     int w = 0;
     if (lane == 0 && A.out_cap) {
       const uint32_t idle = *(volatile uint32_t*)&A.ctr[4 * kCtrStride];
       if (idle) {
         const uint32_t tail = *(volatile uint32_t*)&A.ctr[1 * kCtrStride], head = *(volatile uint32_t*)&A.ctr[2 * kCtrStride];
-        w = (tail - min(head, tail) < idle) && clock64() - t_start > A.budget;
+        w = (tail - min(head, tail) < idle) && (long long)(uint32_t(clock()) - t_start) > A.budget;
       }
     }
     return __shfl_sync(kFull, w, 0) != 0;
@@ -422,6 +415,119 @@ __global__ void __launch_bounds__(kEnumWarps * 32, kEnumMinBlocks) enumerate_ker
         else if (lane == lv) dst[col] = leaf;
       }
     }
+  };
+
+  // Scans the driver windows of depth lv, 32 entries at a time, one per lane:
+  // the depth's candidate bitmap, injectivity against earlier depths of the
+  // same label, then membership in the other backward segments.  What does not
+  // change from window to window -- the bitmap's place, the driver range's
+  // end, the backward segments' bounds (with their cursors), and at the leaf
+  // the positions of the same-label mapped vertices in the driver range -- is
+  // read once per scan.  A non-leaf scan stops at the first window that leaves
+  // candidates (they go to the depth's buffer); a leaf scan consumes the whole
+  // range, adding embeddings.  Every 64 windows the query's work limit and the
+  // idle warps are checked.  Returns false when the query is over its limit.
+  auto scan = [&](uint32_t d, uint32_t lv, bool leaf, uint32_t t_start, uint32_t& steps) -> bool {
+    const uint32_t dv = __shfl_sync(kFull, drv, lv);
+    const uint32_t de = __shfl_sync(kFull, dend, lv);
+    uint32_t dp = __shfl_sync(kFull, dpos, lv);
+    const uint32_t bmbase = ws.plan.bmbase[lv];
+    const uint32_t* __restrict__ bm = A.pool + ws.plan.bmoff[lv];
+    const uint32_t bw = ws.plan.bwd[lv] & ~(1u << dv);
+    const uint32_t same = ws.plan.same[lv];
+    uint32_t seg_lo = 0, seg_hi = 0;
+    if ((bw >> lane) & 1u) {
+      const uint32_t* s = g.lseg + uint64_t(f) * W1 + ws.plan.lab[lv];
+      seg_lo = s[0];
+      seg_hi = s[1];
+      bytes += 8;
+    }
+    // Leaf: lane j of the same-label depths holds the position of f_j in the
+    // driver range (kInvalid when absent); the range has no repeated entry, so
+    // f_j can only be the entry at that position.
+    uint32_t same_pos = kInvalid;
+    unsigned long long Sp = 0;
+    uint64_t tq = 0;
+    if (leaf) {
+      if ((same >> lane) & 1u) {
+        uint32_t lo = dp, hi = de;
+        while (lo < hi) {
+          const uint32_t mid = (lo + hi) >> 1;
+          const uint32_t y = __ldg(g.adj + mid);
+          bytes += 4;
+          if (y < f) lo = mid + 1;
+          else if (y > f) hi = mid;
+          else { same_pos = mid; break; }
+        }
+      }
+      Sp = __shfl_sync(kFull, S, lv - 1);
+      tq = uint64_t(ws.plan.qv[lv]) << 32;
+    }
+    while (dp < de) {
+      const uint32_t nvalid = min(32u, de - dp);
+      const uint32_t k = dp + lane;
+      bool pred = lane < nvalid;
+      const uint32_t x = pred ? __ldg(g.adj + k) : 0xffffffffu;
+      const uint32_t xo = (pred && leaf) ? __ldg(g.adj_old + k) : 0u;
+      if (pred) bytes += leaf ? 8 : 4;
+      if (pred) {
+        const uint32_t bit = x - bmbase;
+        pred = (__ldg(bm + (bit >> 5)) >> (bit & 31)) & 1u;
+        bytes += 4;
+      }
+      if (leaf) {
+        uint32_t hit = __ballot_sync(kFull, same_pos - dp < nvalid);
+        while (hit) {
+          const uint32_t j = __ffs(hit) - 1;
+          hit &= hit - 1;
+          if (lane == __shfl_sync(kFull, same_pos, j) - dp) pred = false;
+        }
+      } else {
+        uint32_t sm = same;
+        while (sm) {
+          const uint32_t j = __ffs(sm) - 1;
+          sm &= sm - 1;
+          const uint32_t fj = __shfl_sync(kFull, f, j);  // every lane shuffles; then the test
+          pred = pred && x != fj;
+        }
+      }
+      pred = member(bw, x, pred, seg_lo, seg_hi);
+      if (lane == 0) {
+        n_examine++;
+        if (A.work_cap) pend += nvalid;
+      }
+      dp += kChunk;
+      const uint32_t m = __ballot_sync(kFull, pred);
+      if (leaf) {
+        if (pred) {
+          my_count += 1;
+          my_hash += fmix64(A.seed + Sp + fmix64(tq | xo));
+        }
+        if (A.emit && m) emit_rows(m, lv, xo);
+        if (lane == lv) lc += __popc(m);
+      } else if (m) {
+        __syncwarp();
+        if (pred) ws.cand[lv][__popc(m & lanemask_lt())] = x;
+        __syncwarp();
+        if (lane == lv) {
+          dpos = dp;
+          cnt = __popc(m);
+          it = 0;
+          lc += __popc(m);
+        }
+        return true;
+      }
+      if ((++steps & 63u) == 0) {
+        if (lane == lv) dpos = dp;
+        if (over_limit()) return false;
+        if (should_split(t_start)) {
+          donate(d, lv);
+          dp = __shfl_sync(kFull, dpos, lv);  // this depth's range may have been handed off
+        }
+      }
+    }
+    if (lane == lv) dpos = dp;
+    return true;
   };
 
   // Runs one task: depth d, mapped f (lane-distributed, lanes < d), driver
@@ -455,7 +561,7 @@ __global__ void __launch_bounds__(kEnumWarps * 32, kEnumMinBlocks) enumerate_ker
       return;
     }
     if (A.work_cap && over_limit()) return;
-    const long long t_start = clock64();
+    const uint32_t t_start = uint32_t(clock());
     uint32_t lv = d;
     enter(d, lo_set, hi_set);
     uint32_t steps = 0;
@@ -465,24 +571,7 @@ __global__ void __launch_bounds__(kEnumWarps * 32, kEnumMinBlocks) enumerate_ker
         if (should_split(t_start)) donate(d, lv);
       }
       if (lv == n - 1) {
-        const unsigned long long Sp = __shfl_sync(kFull, S, lv - 1);
-        const uint64_t tb = uint64_t(ws.plan.qv[lv]) << 32;
-        uint32_t leaf_cur = 0;  // lane j: search start in backward segment j
-        while (__shfl_sync(kFull, dpos, lv) < __shfl_sync(kFull, dend, lv)) {
-          uint32_t x, xo;
-          const bool p = examine(lv, true, x, xo, leaf_cur);
-          const uint32_t m = __ballot_sync(kFull, p);
-          if (p) {
-            my_count += 1;
-            my_hash += fmix64(A.seed + Sp + fmix64(tb | xo));
-          }
-          if (A.emit && m) emit_rows(m, lv, xo);
-          if (lane == lv) lc += __popc(m);
-          if ((++steps & 63u) == 0) {
-            if (over_limit()) return;
-            if (should_split(t_start)) donate(d, lv);
-          }
-        }
+        if (!scan(d, lv, true, t_start, steps)) return;
         if (lv == d) return;
         lv--;
         continue;
@@ -502,18 +591,7 @@ __global__ void __launch_bounds__(kEnumWarps * 32, kEnumMinBlocks) enumerate_ker
         continue;
       }
       if (__shfl_sync(kFull, dpos, lv) < __shfl_sync(kFull, dend, lv)) {
-        uint32_t x, xo;
-        uint32_t no_cur = 0;
-        const bool p = examine(lv, false, x, xo, no_cur);
-        const uint32_t m = __ballot_sync(kFull, p);
-        __syncwarp();
-        if (p) ws.cand[lv][__popc(m & lanemask_lt())] = x;
-        __syncwarp();
-        if (lane == lv) {
-          cnt = __popc(m);
-          it = 0;
-          lc += __popc(m);
-        }
+        if (!scan(d, lv, false, t_start, steps)) return;
         continue;
       }
       if (lv == d) return;
@@ -581,9 +659,10 @@ __global__ void __launch_bounds__(kEnumWarps * 32, kEnumMinBlocks) enumerate_ker
       atomicSub(&A.ctr[5 * kCtrStride], 1u);
       const uint32_t waiting = atomicAdd(&A.ctr[4 * kCtrStride], 1u);
       uint32_t sleep_ns = 256;
-      // enough warps already wait: leave (queued work is never lost)
-      const uint32_t limit = waiting >= kMaxWaiters ? 1u : kIdleSpinLimit;
-      for (uint32_t spin = 0; spin < limit; spin++) {
+      // enough warps already wait: leave at once (queued work is never lost)
+      const unsigned long long t_idle = global_ns();
+      const unsigned long long idle_ns = waiting >= kMaxWaiters ? 0ull : A.idle_wait_ns;
+      for (;;) {
         const uint32_t tail = min(*(volatile uint32_t*)&A.ctr[1 * kCtrStride], A.out_cap);
         uint32_t h = *(volatile uint32_t*)&A.ctr[2 * kCtrStride];
         bool got = false;
@@ -597,16 +676,20 @@ __global__ void __launch_bounds__(kEnumWarps * 32, kEnumMinBlocks) enumerate_ker
         if (*(volatile uint32_t*)&A.ctr[5 * kCtrStride] == 0 &&
             *(volatile uint32_t*)&A.ctr[2 * kCtrStride] >= min(*(volatile uint32_t*)&A.ctr[1 * kCtrStride], A.out_cap))
           break;
-        if (spin + 1 == limit) break;
+        if (global_ns() - t_idle >= idle_ns) break;
         __nanosleep(sleep_ns);
         if (sleep_ns < 8192) sleep_ns <<= 1;
       }
       atomicSub(&A.ctr[4 * kCtrStride], 1u);
       if (slot != kInvalid) {
         atomicAdd(&A.ctr[5 * kCtrStride], 1u);
-        uint32_t spins = 0;
+        const unsigned long long t_ready = global_ns();
         while (*(volatile uint32_t*)&A.out_ready[slot] != A.tag) {
-          if (++spins > kReadySpinLimit) { atomicOr(&A.ctr[3 * kCtrStride], kErrTimeout); slot = kInvalid - 1; break; }
+          if (global_ns() - t_ready > A.ready_wait_ns) {
+            atomicOr(&A.ctr[3 * kCtrStride], kErrTimeout);
+            slot = kInvalid - 1;
+            break;
+          }
           __nanosleep(64);
         }
         if (slot == kInvalid - 1) atomicSub(&A.ctr[5 * kCtrStride], 1u);
@@ -623,11 +706,11 @@ __global__ void __launch_bounds__(kEnumWarps * 32, kEnumMinBlocks) enumerate_ker
   bytes = warp_sum(bytes);
   if (lane == 0) {
     atomicAdd(A.algo_bytes, bytes);
-    atomicAdd(&A.ev[0], n_tasks);
-    atomicAdd(&A.ev[1], n_pops);
-    atomicAdd(&A.ev[2], n_handoffs);
-    atomicAdd(&A.ev[3], n_recs);
-    atomicAdd(&A.ev[4], n_examine);
+    atomicAdd(&A.ev[0], (unsigned long long)n_tasks);
+    atomicAdd(&A.ev[1], (unsigned long long)n_pops);
+    atomicAdd(&A.ev[2], (unsigned long long)n_handoffs);
+    atomicAdd(&A.ev[3], (unsigned long long)n_recs);
+    atomicAdd(&A.ev[4], (unsigned long long)n_examine);
   }
 }
 

@@ -1,7 +1,12 @@
 // Seeded synthetic workloads: R-MAT and Chung-Lu data graphs, uniform and
-// Zipf labels, random-walk queries, and a t/v/e writer.  Host code only; the
-// same source gives the same graphs on x86-64 and AArch64 (integer RNG; the
-// only libm call is pow() in the Chung-Lu weights).
+// Zipf labels, random-walk queries, and a t/v/e writer.  Host code only.
+//
+// The same source gives bit-identical graphs on x86-64 and AArch64: the RNG is
+// integer, the floating point uses only +, -, *, / and sqrt (correctly
+// rounded on both), the powers in the Chung-Lu weights and Zipf labels come
+// from det_pow below instead of libm (whose last bit may differ between
+// platforms), and the file is compiled with -ffp-contract=off so that no
+// multiply-add is fused on one platform and not the other.
 #include "../../include/fsig_gen.h"
 
 #include <algorithm>
@@ -15,6 +20,39 @@
 #include <vector>
 
 namespace {
+
+// x^y for x >= 1 and moderate |y|, from the series definitions alone:
+//   ln x = e ln 2 + 2 atanh(t),  t = (m - 1) / (m + 1),  x = m 2^e, m in [1/sqrt2, sqrt2)
+//   atanh t = sum t^(2k+1) / (2k+1)                   (|t| < 0.172, 16 terms)
+//   exp z   = 2^k exp(r),  r = z - k ln 2, |r| <= ln2/2, exp r = sum r^j / j!  (24 terms)
+// Relative error about 1e-15, which is ample for weights; what matters is
+// that every step is a basic IEEE operation, so both platforms agree bit for
+// bit.
+double det_pow(double x, double y) {
+  constexpr double kLn2 = 0.693147180559945309417232121458;
+  constexpr double kSqrtHalf = 0.707106781186547524400844362105;
+  int e = 0;
+  double m = std::frexp(x, &e);  // exact: x = m 2^e, m in [0.5, 1)
+  if (m < kSqrtHalf) {
+    m *= 2.0;
+    e -= 1;
+  }
+  const double t = (m - 1.0) / (m + 1.0), t2 = t * t;
+  double term = t, s = 0.0;
+  for (int k = 0; k < 16; k++) {
+    s += term / double(2 * k + 1);
+    term *= t2;
+  }
+  const double z = y * (double(e) * kLn2 + 2.0 * s);
+  const double kf = std::floor(z / kLn2 + 0.5);
+  const double r = z - kf * kLn2;
+  double p = 1.0, acc = 1.0;
+  for (int j = 1; j < 24; j++) {
+    p = p * r / double(j);
+    acc += p;
+  }
+  return std::ldexp(acc, int(kf));  // exact scaling by a power of two
+}
 
 inline uint64_t splitmix64(uint64_t& s) {
   uint64_t z = (s += 0x9e3779b97f4a7c15ull);
@@ -140,7 +178,7 @@ int fsig_gen_chung_lu(uint32_t V, uint64_t E, double gamma, uint64_t seed, int t
   const double alpha = 1.0 / (gamma - 1.0);
   std::vector<double> w(V);
   double sum = 0;
-  for (uint32_t i = 0; i < V; i++) sum += (w[i] = std::pow(double(i) + 1.0, -alpha));
+  for (uint32_t i = 0; i < V; i++) sum += (w[i] = det_pow(double(i) + 1.0, -alpha));
   const double target = 2.0 * double(E), cap = std::sqrt(target);
   // Scale to the target total degree; cap at sqrt(2E) and rescale the rest.
   for (int it = 0; it < 8; it++) {
@@ -205,7 +243,7 @@ int fsig_gen_labels_zipf(uint32_t V, uint32_t L, double s, uint64_t seed, int32_
   if (!labels || L == 0) return FSIG_GEN_EINVAL;
   std::vector<double> cdf(L);
   double acc = 0;
-  for (uint32_t k = 0; k < L; k++) cdf[k] = (acc += 1.0 / std::pow(double(k) + 1.0, s));
+  for (uint32_t k = 0; k < L; k++) cdf[k] = (acc += 1.0 / det_pow(double(k) + 1.0, s));
   Rng r(seed);
   for (uint32_t i = 0; i < V; i++) {
     double x = r.uniform() * acc;

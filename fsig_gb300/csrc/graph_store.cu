@@ -13,7 +13,6 @@ namespace fsig {
 namespace {
 
 constexpr int kRenumTile = 1024;
-constexpr int kMaxLabels = 4096;
 
 // ---- label validation --------------------------------------------------------
 __global__ void label_range_kernel(const int32_t* __restrict__ lab, uint32_t V, int32_t* out_max,
@@ -394,7 +393,7 @@ int build_device_graph(Engine& e, uint32_t V, const int32_t* h_labels, uint64_t 
   FSIG_CUDA_TRY(cudaStreamSynchronize(s));
   if (hf[0] & 1u) return fail(FSIG_EINVAL, "negative vertex label");
   const int32_t L = int32_t(hf[1]) + 1;
-  if (L > kMaxLabels) return fail(FSIG_EINVAL, "more than 4096 distinct labels");
+  if (L > int32_t(kMaxLabels)) return fail(FSIG_EINVAL, "more than 4096 distinct labels");
   g.L = L;
 
   // Renumber by (label, caller id).

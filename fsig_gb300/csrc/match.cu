@@ -43,51 +43,118 @@ GraphView view_of(const DeviceGraph& g) {
 }
 
 // ---------------------------------------------------------------------------
-// Filter: one warp per aligned group of 32 (renumbered) data vertices.  The
-// group's vertices carry one or a few labels (ids are label-sorted); for each
-// query vertex of such a label the warp evaluates the tests lane-parallel and
-// writes one bitmap word with a ballot.  Every bitmap word is written exactly
-// once, so no clearing pass is needed.
+// Filter: one warp per aligned group of 32 (renumbered) data vertices, lane i
+// holding vertex i of the group.  The group's vertices carry one or a few
+// labels (ids are label-sorted).  The warp turns its 32 signatures around
+// once: after a 32 x 32 bit transpose of each signature word (five rounds of
+// shuffles), lane b holds, for word w, the mask of the group's vertices whose
+// word w has bit b set, kept in shared memory.  The query vertices of each of
+// the group's labels are then taken 32 at a time, one per lane: a lane ANDs
+// the masks of the signature bits its query vertex requires (subset test,
+// GSI_kernels.cuh:8-24), the label mask and the mask of vertices of at least
+// its degree (initialise_kernel, MMatch_kernels.cuh:6-16), which is the
+// query vertex's bitmap word for this group, written once.  Every bitmap word
+// is written exactly once, so no clearing pass is needed.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) filter_kernel(GraphView g, const QVert* __restrict__ qv,
-                                                     const uint32_t* __restrict__ lab_gidx,
-                                                     const uint32_t* __restrict__ lab_begin, uint32_t mode,
-                                                     uint32_t* __restrict__ pool) {
+constexpr uint32_t kFilterWarps = 8;
+
+__device__ __forceinline__ uint32_t transpose_step(uint32_t x, uint32_t lane, uint32_t j, uint32_t m) {
+  const uint32_t y = __shfl_xor_sync(kFull, x, j);
+  return (lane & j) ? ((x & ~m) | ((y >> j) & m)) : ((x & m) | ((y << j) & ~m));
+}
+
+// Lane b receives bit b of every lane's x: bit i of the result = bit b of
+// lane i's x (32 x 32 bit-matrix transpose).
+__device__ __forceinline__ uint32_t warp_transpose32(uint32_t x, uint32_t lane) {
+  x = transpose_step(x, lane, 16, 0x0000ffffu);
+  x = transpose_step(x, lane, 8, 0x00ff00ffu);
+  x = transpose_step(x, lane, 4, 0x0f0f0f0fu);
+  x = transpose_step(x, lane, 2, 0x33333333u);
+  x = transpose_step(x, lane, 1, 0x55555555u);
+  return x;
+}
+
+__global__ void __launch_bounds__(kFilterWarps * 32, 4) filter_kernel(GraphView g, const QVert* __restrict__ qv,
+                                                                   const uint32_t* __restrict__ lab_gidx,
+                                                                   const uint32_t* __restrict__ lab_begin,
+                                                                   uint32_t mode, uint32_t* __restrict__ pool) {
+  __shared__ uint32_t cols[kFilterWarps][kSigWords - 1][32];
   const uint32_t lane = threadIdx.x & 31;
+  uint32_t (*col)[32] = cols[threadIdx.x >> 5];
   const uint32_t nwt = (gridDim.x * blockDim.x) >> 5;
   const uint32_t ngroups = (g.V + 31) >> 5;
+  const bool use_sig = mode & kFilterSignature, use_deg = mode & kFilterDegree;
   for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < ngroups; w += nwt) {
     const uint32_t v = (w << 5) + lane;
     const bool live = v < g.V;
     const int32_t l = live ? g.label[v] : -1;
-    const uint32_t deg = live ? g.off[v + 1] - g.off[v] : 0;
-    uint4 s0 = make_uint4(0, 0, 0, 0), s1 = s0, s2 = s0, s3 = s0;
-    if ((mode & kFilterSignature) && live) {
-      const uint4* p = g.sig + uint64_t(v) * 4;
-      s0 = p[0]; s1 = p[1]; s2 = p[2]; s3 = p[3];
+    // lane t: the group's vertices of degree >= t (query degrees are < 32)
+    uint32_t atleast = kFull;
+    if (use_deg) {
+      const uint32_t deg = live ? g.off[v + 1] - g.off[v] : 0;
+#pragma unroll 4
+      for (uint32_t t = 0; t < 32; t++) {
+        const uint32_t m = __ballot_sync(kFull, deg >= t);
+        if (lane == t) atleast = m;
+      }
+    }
+    if (use_sig) {
+      uint4 s0 = make_uint4(0, 0, 0, 0), s1 = s0, s2 = s0, s3 = s0;
+      if (live) {
+        const uint4* p = g.sig + uint64_t(v) * 4;
+        s0 = p[0]; s1 = p[1]; s2 = p[2]; s3 = p[3];
+      }
+      __syncwarp();
+      // word 0 is the label; words 1..15 hold the neighbour-label counters
+      col[0][lane] = warp_transpose32(s0.y, lane);
+      col[1][lane] = warp_transpose32(s0.z, lane);
+      col[2][lane] = warp_transpose32(s0.w, lane);
+      col[3][lane] = warp_transpose32(s1.x, lane);
+      col[4][lane] = warp_transpose32(s1.y, lane);
+      col[5][lane] = warp_transpose32(s1.z, lane);
+      col[6][lane] = warp_transpose32(s1.w, lane);
+      col[7][lane] = warp_transpose32(s2.x, lane);
+      col[8][lane] = warp_transpose32(s2.y, lane);
+      col[9][lane] = warp_transpose32(s2.z, lane);
+      col[10][lane] = warp_transpose32(s2.w, lane);
+      col[11][lane] = warp_transpose32(s3.x, lane);
+      col[12][lane] = warp_transpose32(s3.y, lane);
+      col[13][lane] = warp_transpose32(s3.z, lane);
+      col[14][lane] = warp_transpose32(s3.w, lane);
+      __syncwarp();
     }
     const int32_t lfirst = __shfl_sync(kFull, l, 0);
     const uint32_t last_lane = min(31u, g.V - 1 - (w << 5));
     const int32_t llast = __shfl_sync(kFull, l, last_lane);
     for (int32_t lab = lfirst; lab <= llast; lab++) {
+      const uint32_t lmask = __ballot_sync(kFull, l == lab);
       const uint32_t b = lab_begin[lab], e = lab_begin[lab + 1];
-      for (uint32_t i = b; i < e; i++) {
-        const QVert* q = qv + lab_gidx[i];
-        bool p = l == lab;
-        if (mode & kFilterDegree) p = p && deg >= q->deg;
-        if (mode & kFilterSignature) {
-          const uint4* qs = reinterpret_cast<const uint4*>(q->sig);
-          uint4 a = qs[0], bb = qs[1], c = qs[2], d = qs[3];
-          // word 0 (the label) is covered by l == lab
-          bool sub = ((a.y & s0.y) == a.y) & ((a.z & s0.z) == a.z) & ((a.w & s0.w) == a.w) &
-                     ((bb.x & s1.x) == bb.x) & ((bb.y & s1.y) == bb.y) & ((bb.z & s1.z) == bb.z) &
-                     ((bb.w & s1.w) == bb.w) & ((c.x & s2.x) == c.x) & ((c.y & s2.y) == c.y) &
-                     ((c.z & s2.z) == c.z) & ((c.w & s2.w) == c.w) & ((d.x & s3.x) == d.x) &
-                     ((d.y & s3.y) == d.y) & ((d.z & s3.z) == d.z) & ((d.w & s3.w) == d.w);
-          p = p && sub;
+      for (uint32_t i0 = b; i0 < e; i0 += 32) {
+        const uint32_t i = i0 + lane;
+        uint32_t word = 0, qdeg = 0;
+        const QVert* q = nullptr;
+        if (i < e) {
+          q = qv + lab_gidx[i];
+          word = lmask;
+          qdeg = min(q->deg, 31u);
+          if (use_sig) {
+            // word 0 (the label) is covered by the label mask
+#pragma unroll
+            for (int k = 1; k < kSigWords; k++) {
+              uint32_t need = q->sig[k];
+              while (need) {
+                const uint32_t bit = __ffs(need) - 1;
+                need &= need - 1;
+                word &= col[k - 1][bit];
+              }
+            }
+          }
         }
-        const uint32_t word = __ballot_sync(kFull, p);
-        if (lane == 0 && q->words) pool[q->bmoff + (w - (q->bmbase >> 5))] = word;
+        const uint32_t dm = __shfl_sync(kFull, atleast, qdeg);
+        if (i < e) {
+          if (use_deg) word &= dm;
+          if (q->words) pool[q->bmoff + (w - (q->bmbase >> 5))] = word;
+        }
       }
     }
   }
@@ -105,13 +172,17 @@ __global__ void __launch_bounds__(256) filter_kernel(GraphView g, const QVert* _
 // every vertex its own class every k is one.  A class dominated by u's (dom)
 // is tested first: C(u) stays within C(dom) through the refinement, so a v
 // outside C(dom) fails one of the counts anyway.  Warps take runs of bitmap
-// words; class members other than the smallest own no words.
+// words (lane = candidate); class members other than the smallest own no
+// words.  A candidate's segment of at most coop_min entries is scanned by its
+// own lane; a longer one by the whole warp, 32 consecutive entries per step
+// (coalesced loads, one ballot per step), one such candidate after another.
 // ---------------------------------------------------------------------------
 constexpr uint32_t kRefineRun = 8;
 
 __global__ void __launch_bounds__(256) refine_kernel(GraphView g, const QVert* __restrict__ qv, uint32_t G,
                                                      const uint64_t* __restrict__ gword, uint64_t total_words,
-                                                     const uint32_t* __restrict__ src, uint32_t* __restrict__ dst) {
+                                                     const uint32_t* __restrict__ src, uint32_t* __restrict__ dst,
+                                                     uint32_t coop_min) {
   const uint32_t lane = threadIdx.x & 31;
   const uint64_t nwt = (uint64_t(gridDim.x) * blockDim.x) >> 5;
   const uint64_t W1 = uint64_t(g.L) + 1;
@@ -149,20 +220,43 @@ __global__ void __launch_bounds__(256) refine_kernel(GraphView g, const QVert* _
         const uint32_t grp = m & qw->cmask;
         m &= ~grp;
         const uint32_t need = __popc(grp);
+        if (qw->words == 0) {  // no data vertex carries the neighbour's label
+          alive = false;
+          continue;
+        }
+        const uint32_t* __restrict__ nb = src + qw->bmoff;
+        const uint32_t nbase = qw->bmbase;
+        uint32_t k = 0, e = 0;
         if (alive) {
-          if (qw->words == 0) {
-            alive = false;
-          } else {
-            const uint32_t* s = g.lseg + uint64_t(v) * W1 + qw->label;
-            uint32_t k = s[0];
-            const uint32_t e = s[1];
-            uint32_t have = 0;
-            for (; k < e && have < need; k++) {
-              const uint32_t bit = g.adj[k] - qw->bmbase;
-              have += (src[qw->bmoff + (bit >> 5)] >> (bit & 31)) & 1u;
-            }
-            alive = have >= need;
+          const uint32_t* s = g.lseg + uint64_t(v) * W1 + qw->label;
+          k = s[0];
+          e = s[1];
+        }
+        const bool coop = alive && e - k > coop_min;
+        if (alive && !coop) {
+          uint32_t have = 0;
+          for (; k < e && have < need; k++) {
+            const uint32_t bit = g.adj[k] - nbase;
+            have += (nb[bit >> 5] >> (bit & 31)) & 1u;
           }
+          alive = have >= need;
+        }
+        uint32_t cm = __ballot_sync(kFull, coop);
+        while (cm) {
+          const uint32_t c = __ffs(cm) - 1;
+          cm &= cm - 1;
+          const uint32_t ck = __shfl_sync(kFull, k, c), ce = __shfl_sync(kFull, e, c);
+          uint32_t have = 0;
+          for (uint32_t p = ck; p < ce && have < need; p += 32) {
+            const uint32_t idx = p + lane;
+            bool hit = false;
+            if (idx < ce) {
+              const uint32_t bit = g.adj[idx] - nbase;
+              hit = (nb[bit >> 5] >> (bit & 31)) & 1u;
+            }
+            have += __popc(__ballot_sync(kFull, hit));
+          }
+          if (lane == c) alive = have >= need;
         }
       }
       const uint32_t nw = __ballot_sync(kFull, alive);
@@ -542,7 +636,7 @@ T* upload(Engine& e, const std::vector<T>& v, int& rc) {
 // Filter + refine + popcount on the device.  Returns the final pool.
 int filter_stage(Engine& e, const BatchLayout& b, uint32_t mode, int refine_iters, QVert* d_qv, uint64_t* d_gword,
                  uint32_t* d_lab_gidx, uint32_t* d_lab_begin, uint32_t*& pool, uint32_t* d_counts,
-                 uint32_t* launches = nullptr) {
+                 uint32_t* launches = nullptr, uint32_t coop_min = kRefineCoopDefault) {
   uint32_t nl = 1;
   const DeviceGraph& g = e.g;
   cudaStream_t s = e.stream;
@@ -550,14 +644,15 @@ int filter_stage(Engine& e, const BatchLayout& b, uint32_t mode, int refine_iter
   uint32_t* p1 = refine_iters > 0 ? e.arena.take<uint32_t>(std::max<uint64_t>(b.words, 1)) : nullptr;
   if (!p0 || (refine_iters > 0 && !p1)) return fail(FSIG_EADMISSION, "candidate bitmaps do not fit the arena");
   const GraphView gv = view_of(g);
-  filter_kernel<<<grid_cap(uint64_t(g.V), 256, e.num_sms, 16), 256, 0, s>>>(gv, d_qv, d_lab_gidx, d_lab_begin, mode,
-                                                                           p0);
+  filter_kernel<<<grid_cap(uint64_t(g.V), kFilterWarps * 32, e.num_sms, 8), kFilterWarps * 32, 0, s>>>(
+      gv, d_qv, d_lab_gidx, d_lab_begin, mode, p0);
   FSIG_CUDA_TRY(cudaGetLastError());
   uint32_t* cur = p0;
   uint32_t* nxt = p1;
   for (int it = 0; it < refine_iters && b.words; it++) {
     const uint64_t runs = (b.words + kRefineRun - 1) / kRefineRun;
-    refine_kernel<<<grid_cap(runs * 32, 256, e.num_sms, 16), 256, 0, s>>>(gv, d_qv, b.G, d_gword, b.words, cur, nxt);
+    refine_kernel<<<grid_cap(runs * 32, 256, e.num_sms, 16), 256, 0, s>>>(gv, d_qv, b.G, d_gword, b.words, cur, nxt,
+                                                                           coop_min);
     FSIG_CUDA_TRY(cudaGetLastError());
     std::swap(cur, nxt);
     nl++;
@@ -712,6 +807,10 @@ int enum_prepare(Engine& e, const BatchOptions& opt, const GraphView& gv, const 
   A.algo_bytes = d_misc + 1;
   A.ev = R.d_ev;
   A.seed = FSIG_HASH_SEED;
+  A.ready_wait_ns = e.ready_wait_ns;
+  A.idle_wait_ns = e.idle_wait_ns;
+  A.unpublished = e.inject_unpublished;
+  A.isect = opt.isect;
   R.out = qa;
   R.ready = ra;
   R.other = qb;
@@ -816,10 +915,15 @@ int run_batch(Engine& e, const std::vector<HostQuery>& qs, const BatchOptions& o
   out.ok.assign(Q, 0);
   if (Q == 0) return FSIG_OK;
   if (b.root_cap + 1 > 0xffffffffull) return fail(FSIG_EADMISSION, "batch has more than 2^32 root candidates");
-  if (opt.emit_cap && Q != 1) return fail(FSIG_EINVAL, "embedding output is for one query at a time");
+  if ((opt.emit_cap || opt.want_tasks) && Q != 1)
+    return fail(FSIG_EINVAL, "embedding output and task ranges are for one query at a time");
   // One CUDA graph per batch when every step is stream-ordered: orders chosen
   // on the device and no embedding output.
-  const bool graph = opt.use_graph && !opt.host_order && !opt.emit_cap;
+  const bool graph = opt.use_graph && !opt.host_order && !opt.emit_cap && !opt.want_tasks;
+  // The host writes this batch into the page-locked staging area that earlier
+  // calls' copies read from the stream: wait until the stream has drained
+  // (every call also drains it before it returns, errors included).
+  FSIG_CUDA_TRY(cudaStreamSynchronize(s));
   e.arena.release(g.arena_mark);
   e.cur_h2d = 0;
   uint64_t d2h = 0;
@@ -900,7 +1004,7 @@ int run_batch(Engine& e, const std::vector<HostQuery>& qs, const BatchOptions& o
 
     uint32_t* pool = nullptr;
     rc = filter_stage(e, b, opt.filter_mode, opt.refine_iters, d_qv, d_gword, d_lab_gidx, d_lab_begin, pool,
-                      d_counts, &launches);
+                      d_counts, &launches, opt.refine_coop);
     if (rc) return rc;
     FSIG_CUDA_TRY(record(e.ev[1], s));
 
@@ -1067,7 +1171,12 @@ int run_batch(Engine& e, const std::vector<HostQuery>& qs, const BatchOptions& o
     }
   } else {
     rc = enqueue();
-    if (rc) return rc;
+    if (rc) {
+      // work queued before the failure still reads the staging area and the
+      // arena: let it finish before they are reused
+      cudaStreamSynchronize(s);
+      return rc;
+    }
     do {
       FSIG_CUDA_TRY(cudaStreamSynchronize(s));
       out.passes++;
@@ -1078,19 +1187,23 @@ int run_batch(Engine& e, const std::vector<HostQuery>& qs, const BatchOptions& o
         if (rc) return rc;
       }
     } while (more);
-    if (opt.emit_cap) {
+    if (opt.emit_cap || opt.want_tasks) {
       uint32_t nroots = 0;
       FSIG_CUDA_TRY(cudaMemcpyAsync(&nroots, d_rootoff + Q, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-      FSIG_CUDA_TRY(cudaMemcpyAsync(&out.emit_total, d_emit_ctr, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+      if (opt.emit_cap)
+        FSIG_CUDA_TRY(cudaMemcpyAsync(&out.emit_total, d_emit_ctr, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
       FSIG_CUDA_TRY(cudaStreamSynchronize(s));
       FSIG_CUDA_TRY(cudaMemcpyAsync(&out.tasks_total, d_chunk_off + nroots, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
       FSIG_CUDA_TRY(cudaStreamSynchronize(s));
+      d2h += 8;
+    }
+    if (opt.emit_cap) {
       const uint64_t rows = std::min<uint64_t>(out.emit_total, opt.emit_cap);
       out.rows.resize(rows * qs[0].n);
       if (rows)
         FSIG_CUDA_TRY(cudaMemcpyAsync(out.rows.data(), d_emit, sizeof(uint32_t) * rows * qs[0].n,
                                       cudaMemcpyDeviceToHost, s));
-      d2h += 16 + sizeof(uint32_t) * rows * qs[0].n;
+      d2h += 8 + sizeof(uint32_t) * rows * qs[0].n;
     }
     rc = copy_back();
     if (rc) return rc;
@@ -1298,6 +1411,11 @@ namespace fsig {
 namespace {
 constexpr uint64_t kNoAllocPoolWords = 1ull << 21;
 constexpr uint64_t kNoAllocMetaWords = 8192;
+// The metadata region holds the label group table (L + 1 words), the query's
+// vertex list (<= 32 words) and its descriptors (32 x 28 words), with slack
+// for their 16-byte alignment: 7199 labels fit, more than a loaded graph has.
+constexpr uint64_t kNoAllocMaxLabels = kNoAllocMetaWords - 1 - kMaxQ - sizeof(QVert) / 4 * kMaxQ - 64;
+static_assert(kMaxLabels <= kNoAllocMaxLabels, "every loadable graph's label table fits the metadata region");
 static __device__ __align__(256) uint32_t g_noalloc_scratch[kNoAllocPoolWords + kNoAllocMetaWords];
 
 constexpr int kNoAllocMaxDevices = 64;
@@ -1342,8 +1460,9 @@ int run_filter_noalloc(Engine& e, const fsig_query& q, uint32_t filter_mode, uin
   const DeviceGraph& g = e.g;
   if (q.num_vertices == 0 || q.num_vertices > uint32_t(kMaxQ)) return fail(FSIG_EQUERY, "query size must be 1..32");
   if (!q.labels || (q.num_edges && !q.edges) || !d_flags) return fail(FSIG_EINVAL, "null argument");
-  if (g.L + 1 + kMaxQ + sizeof(QVert) / 4 * kMaxQ + 64 > kNoAllocMetaWords)
-    return fail(FSIG_EADMISSION, "the allocation-free filter supports at most 4096 labels");
+  if (uint64_t(g.L) > kNoAllocMaxLabels)  // guard; a loaded graph has at most kMaxLabels
+    return fail(FSIG_EADMISSION, "the allocation-free filter's label table holds " +
+                                     std::to_string(kNoAllocMaxLabels) + " labels; the graph has " + std::to_string(g.L));
   const uint32_t n = q.num_vertices;
   // Query descriptors on the stack (no host allocation either).
   QVert qv[kMaxQ];
@@ -1409,8 +1528,8 @@ int run_filter_noalloc(Engine& e, const fsig_query& q, uint32_t filter_mode, uin
   FSIG_CUDA_TRY(cudaMemcpyAsync(d_meta, meta, sizeof(uint32_t) * (uint64_t(g.L) + 1 + n), cudaMemcpyHostToDevice, s));
   FSIG_CUDA_TRY(cudaMemcpyAsync(d_qv, qv, sizeof(QVert) * n, cudaMemcpyHostToDevice, s));
   FSIG_CUDA_TRY(cudaMemsetAsync(d_flags, 0, uint64_t(n) * g.V, s));
-  filter_kernel<<<grid_cap(uint64_t(g.V), 256, e.num_sms, 16), 256, 0, s>>>(view_of(g), d_qv, d_meta + g.L + 1,
-                                                                           d_meta, filter_mode, pool);
+  filter_kernel<<<grid_cap(uint64_t(g.V), kFilterWarps * 32, e.num_sms, 8), kFilterWarps * 32, 0, s>>>(
+      view_of(g), d_qv, d_meta + g.L + 1, d_meta, filter_mode, pool);
   FSIG_CUDA_TRY(cudaGetLastError());
   if (words) {
     bitmap_to_flags_kernel<<<grid_cap(words, 256, e.num_sms, 16), 256, 0, s>>>(d_qv, n, pool, words, g.old_of_new,

@@ -81,6 +81,10 @@ struct QueryResult {
   unsigned int pad;
 };
 
+// Refinement: candidate segments longer than this are scanned by the whole
+// warp, shorter ones by the candidate's own lane.
+constexpr uint32_t kRefineCoopDefault = 32;
+
 // Enumeration launch shape: at most kEnumWarps warps per block, compiled for
 // kEnumMinBlocks resident blocks per SM (which caps registers per thread).
 constexpr uint32_t kEnumWarps = 8;
@@ -108,6 +112,13 @@ struct BatchOptions {
   // BatchOutput::rows, and enumerate only pass-0 tasks [task_begin, task_end).
   uint64_t emit_cap = 0;
   uint32_t task_begin = 0, task_end = 0xffffffffu;
+  // Single-query batches: report the size of the pass-0 task space in
+  // BatchOutput::tasks_total (ordinary launches, not a CUDA graph).
+  bool want_tasks = false;
+  // Set-intersection strategy of the enumeration (kIsect* in enumerate.cuh)
+  // and the refinement's lane/warp split (kRefineCoopDefault).
+  uint32_t isect = 0;
+  uint32_t refine_coop = kRefineCoopDefault;
   // Run the batch as one CUDA graph (uploads, filter, order, roots, first
   // enumeration pass, results back) when orders are chosen on the device.
   bool use_graph = false;
@@ -129,7 +140,7 @@ struct BatchOutput {
   float ms_enum = 0;
   std::vector<uint32_t> rows;   // emitted embeddings, n per row (emit_cap > 0)
   uint64_t emit_total = 0;      // embeddings found in the task range
-  uint32_t tasks_total = 0;     // size of the pass-0 task space (emit_cap > 0)
+  uint32_t tasks_total = 0;     // size of the pass-0 task space (emit_cap > 0 or want_tasks)
   bool graph = false;           // ran as a CUDA graph
 };
 

@@ -101,6 +101,17 @@ typedef struct {
   uint32_t no_classes;      /* 1: filter and refine every query vertex on its own,
                                with every neighbour count one; 0 (default):
                                refinement classes (see fsig_refine_classes)      */
+  uint32_t isect;           /* set-intersection strategy of the enumeration:
+                               0 (default) adaptive: the 32 entries after a
+                               segment's cursor first (merge-like), else a
+                               warp-cooperative 32-ary window search; 1 window
+                               search only (galloping-like); 2 every lane
+                               binary-searches the segment alone            */
+  uint32_t refine_coop;     /* refinement: a candidate's neighbour segment
+                               longer than this is scanned by the whole warp
+                               (warp per candidate), shorter ones by the
+                               candidate's own lane (0: default 32;
+                               0xffffffff: always a lane)                    */
 } fsig_batch_opts;
 
 /* ---- engine lifetime; replaces GPUSubgraphMatcher::init_GPU (match/subgraph_match.h:51-80)
@@ -114,7 +125,8 @@ const char* fsig_status_string(int status);
 /* ---- data graph; replaces GraphReader::read (IO/graph_reader.h:27-34) followed by
  *      GraphFormatTransformer::transform (graph_format_transformer/graph_format_transformer.h:37-40)
  *      and MMatch::copy_graph_to_GPU (match/MMatch.cu:14-32).  The CSR, the
- *      label-partitioned adjacency and the signature table are built on the device. ---- */
+ *      label-partitioned adjacency and the signature table are built on the device.
+ *      Labels are 0..4095 (more distinct labels: FSIG_EINVAL). ---- */
 int fsig_load_graph(fsig_engine* e, uint32_t num_vertices, const int32_t* labels,
                     uint64_t num_edges, const uint32_t* edges);
 /* Reads a t/v/e file with the reference reader's semantics (graph_reader.cc:12-55);
@@ -149,6 +161,20 @@ void fsig_free_graph_file(fsig_graph_file* f);
  *      i.e. MMatch::match (match/MMatch.cu:2077-2121, algo 1) and GSI::match
  *      (match/GSI.cu:329-358, algo 2), for one query. ---- */
 int fsig_match(fsig_engine* e, const fsig_query* q, int algo, fsig_result* out);
+/* ---- one query over a range of its root tasks; the block split of
+ *      MMatch::extend_embeddings_recursively (match/MMatch.cu:1834-1985,
+ *      memory_manager.h:220-242) cuts the work of one query into pieces too,
+ *      there to bound memory.  The task space of a query is its root
+ *      candidates in ascending order, each root's first-level driver range in
+ *      chunks of split_len entries (0: 256; at least 32), under the
+ *      algorithm's heuristic order (or q->order).  The call enumerates tasks
+ *      [task_begin, task_end) (task_end may exceed the space) and returns their
+ *      count and set hash in out (level_counts likewise); *tasks_total
+ *      receives the size of the space.  Results of ranges that partition
+ *      [0, tasks_total) add up (counts exactly, hashes modulo 2^64) to the
+ *      query's, so a query can be split across calls, processes or GPUs. ---- */
+int fsig_match_range(fsig_engine* e, const fsig_query* q, int algo, uint32_t split_len, uint32_t task_begin,
+                     uint32_t task_end, fsig_result* out, uint32_t* tasks_total);
 /* Many queries against the resident data graph in one persistent launch.
  * With order_source FSIG_ORDER_LEARNED, a query that carries an order
  * (fsig_query.order) keeps it; the others are ordered by the network. */
@@ -219,6 +245,20 @@ typedef struct {
 } fsig_batch_stats;
 int fsig_last_stats(const fsig_engine* e, fsig_batch_stats* out);
 
+/* ---- bounded waits of the enumeration's work queue (no reference counterpart:
+ *      the reference has no device work queue and ends the process on any
+ *      failure, e.g. memory_manager/memory_manager.h:31-61).  A warp that took
+ *      a handed-off record waits at most ready_wait_ns for it to be published,
+ *      then records FSIG_ETIMEOUT for the call and leaves (0: 200 ms); an idle
+ *      warp waits at most idle_wait_ns for hand-offs before it leaves, its
+ *      share of the queue then running in a later pass (0: 2 s).  unpublished
+ *      = 1 is fault injection for tests: the first record handed off in each
+ *      enumeration pass of later calls is written but never published, so the
+ *      warp that takes it waits out ready_wait_ns and the call returns
+ *      FSIG_ETIMEOUT without faulting the GPU; 0 turns it off.  Waits are
+ *      limited to 60 s. ---- */
+int fsig_set_queue_waits(fsig_engine* e, uint64_t ready_wait_ns, uint64_t idle_wait_ns, int unpublished);
+
 /* ---- transforms with the reference's output layout, built on the device ---- */
 /* UndirectedPlainToCSRTransformer::transform (graph_format_transformer.cc:12-37):
  * offsets[V+1], adj[2E]; rows ascending, duplicate edges kept as the reference keeps them. */
@@ -284,7 +324,9 @@ int fsig_filter_classes(fsig_engine* e, const fsig_query* q, int algo, int refin
  *      d_flags[n * V] (1 = candidate, caller vertex ids); the call clears it
  *      first.  The candidate bitmaps live in a fixed device array of 2^21
  *      words (8 MiB) that every GPU loading the library holds until exit; a
- *      query whose bitmaps need more returns FSIG_EADMISSION.  All calls share
+ *      query whose bitmaps need more returns FSIG_EADMISSION and leaves
+ *      d_flags untouched.  Every graph fsig_load_graph accepts (up to 4096
+ *      labels) fits its label table.  All calls share
  *      the array: calls whose work overlaps on the GPU race.  The first call
  *      on a device looks up the array's address and should come before any
  *      stream capture.  Synchronous: the flags are complete on return. ---- */

@@ -1,6 +1,9 @@
 """Build recipe for the CPU oracle (test infrastructure only).
 
 oracle/_build/liboracle.so   the CPU restatement (oracle.cpp), g++ -O2.
+oracle/_build/libgen.so      a copy of the workload generators
+                             (fsig_gb300/csrc/gen.cpp) for the CPU benchmark
+                             arm, which loads no library of the engine.
 oracle/_ref/ref_dump         the reference's own CPU sources (reader, graph,
                              format transformer, GSI/MMatch host planning)
                              compiled from the reference tree together with
@@ -32,6 +35,19 @@ def build_oracle(force: bool = False) -> Path:
     srcs = [HERE / "oracle.cpp", HERE / "oracle.h"]
     if force or not lib.exists() or lib.stat().st_mtime < max(s.stat().st_mtime for s in srcs):
         _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-pthread", "-o", str(lib), str(HERE / "oracle.cpp")])
+    return lib
+
+
+def build_generators(force: bool = False) -> Path:
+    """The workload generators, built from the engine's source with the same
+    flags (no multiply-add contraction: identical graphs on every platform)."""
+    BUILD.mkdir(exist_ok=True)
+    lib = BUILD / "libgen.so"
+    root = HERE.parent
+    srcs = [root / "fsig_gb300" / "csrc" / "gen.cpp", root / "include" / "fsig_gen.h"]
+    if force or not lib.exists() or lib.stat().st_mtime < max(s.stat().st_mtime for s in srcs):
+        _run(["g++", "-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-shared", "-pthread",
+              "-I", str(root / "include"), "-o", str(lib), str(srcs[0])])
     return lib
 
 
@@ -71,4 +87,5 @@ def build_reference(force: bool = False) -> Path | None:
 
 if __name__ == "__main__":
     print(build_oracle(force="--force" in sys.argv))
+    print(build_generators(force="--force" in sys.argv))
     print(build_reference(force="--force" in sys.argv))

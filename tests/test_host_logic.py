@@ -29,7 +29,8 @@ class KnobEngine:
 
     def match_batch(self, qs, **kw):
         self.ms = 10.0 + abs(kw.get("chunk", 1) - 2) + abs(kw.get("split_len", 256) - 512) / 256 \
-            + (0 if kw.get("warps_per_block", 8) == 8 else 1) + abs(kw.get("split_cycles", 4000) - 16000) / 16000
+            + (0 if kw.get("warps_per_block", 8) == 8 else 1) + abs(kw.get("split_cycles", 4000) - 16000) / 16000 \
+            + 0.5 * abs(kw.get("isect", 0) - 1) + (0.25 if kw.get("refine_coop", 32) != 128 else 0)
         bad = self.broken is not None and kw.get("chunk") == self.broken
         return [FakeResult(i + (1 if bad else 0), 7 * i) for i, _ in enumerate(qs)]
 
@@ -39,8 +40,12 @@ class KnobEngine:
 
 def test_autotune_finds_the_fastest_setting():
     best, trials = autotune.tune(KnobEngine(), [query(3)] * 4, repeats=1)
-    assert best == {"warps_per_block": 8, "chunk": 2, "split_len": 512, "split_cycles": 16000}
+    assert best == {"warps_per_block": 8, "chunk": 2, "split_len": 512, "split_cycles": 16000, "isect": 1}
     assert trials[0][0] == autotune.DEFAULTS
+    # the refinement's warps-per-candidate split joins when the batch refines
+    best, _ = autotune.tune(KnobEngine(), [query(3)] * 4, repeats=1, refine_iters=1)
+    assert best == {"warps_per_block": 8, "chunk": 2, "split_len": 512, "split_cycles": 16000, "isect": 1,
+                    "refine_coop": 128}
 
 
 class WindowEngine(KnobEngine):

@@ -22,10 +22,19 @@ def free_port():
 
 
 def _worker(rank, world, port, out):
+    try:
+        _work(rank, world, port, out)
+    except BaseException as exc:  # report instead of leaving the parent waiting
+        out.put((rank, "error", repr(exc), 0.0, []))
+        raise
+
+
+def _work(rank, world, port, out):
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), WORLD_SIZE=str(world), RANK=str(rank),
                       LOCAL_RANK=str(rank))
     sys.path.insert(0, str(ROOT))
     import bench
+    from fsig_gb300 import workloads as W
     import fsig_gb300 as F
     from oracle import oracle as O
     d = bench.Dist()
@@ -46,8 +55,7 @@ def _worker(rank, world, port, out):
     tot_h = (int(lo) + (int(hi) << 32)) % (1 << 64)
     mx = d.max(float(rank + 1))
     d.barrier()
-    specs = [s[2] for s in bench.candidate_specs("c4", rank)[0][0][:8]]
-    out.put((rank, int(tot_c), tot_h, mx, specs))
+    out.put((rank, int(tot_c), tot_h, mx, W.rank_order(4, rank)))
     d.close()
 
 
@@ -80,6 +88,7 @@ def test_shard_sums_equal_single_process(two_ranks):
         c += cnt
         h = (h + hs) % (1 << 64)
     for rank, tc, th, _, _ in two_ranks:
+        assert tc != "error", th
         assert (tc, th) == (c, h)
 
 
@@ -87,9 +96,8 @@ def test_max_over_ranks(two_ranks):
     assert [r[3] for r in two_ranks] == [2.0, 2.0]
 
 
-def test_ranks_draw_distinct_deterministic_query_seeds(two_ranks):
+def test_ranks_start_at_distinct_batches(two_ranks):
+    """Replicas run the manifest's batches, rank r starting at batch r, so
+    that at any step the ranks work on different queries."""
     s0, s1 = two_ranks[0][4], two_ranks[1][4]
-    assert not set(s0) & set(s1)
-    sys.path.insert(0, str(ROOT))
-    import bench
-    assert [s[2] for s in bench.candidate_specs("c4", 0)[0][0][:8]] == s0
+    assert s0 == [0, 1, 2, 3] and s1 == [1, 2, 3, 0]

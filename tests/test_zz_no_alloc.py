@@ -34,3 +34,54 @@ def test_filter_noalloc_matches_filter_twice():
             got = buf.cpu().numpy().reshape(q.num_vertices, V)
             assert got.sum() > 0
             assert np.array_equal(got, want)
+
+
+def test_filter_noalloc_absent_label_and_limits():
+    """A query label no data vertex carries gives an all-zero row (as
+    fsig_filter does); bitmaps over the fixed array's 2^21 words are refused
+    with FSIG_EADMISSION, the caller's buffer left as it was; the largest
+    label table a loaded graph can have fits."""
+    torch = pytest.importorskip("torch")
+    lab = F.gen_labels(4000, 6, "uniform", seed=12)
+    g = F.gen_rmat(4000, 16000, seed=12, labels=lab)
+    q = F.Query(np.array([0, 999, 2], np.int32), np.array([[0, 1], [1, 2]], np.uint32))
+    with F.Engine(0, arena_bytes=1 << 30) as e:
+        e.load_graph(g)
+        V = e.graph_info()["V"]
+        want = e.filter(q, F.ALGO_GSI, refine_iters=0)
+        buf = torch.full((3 * V,), 7, dtype=torch.uint8, device="cuda:0")
+        torch.cuda.synchronize()
+        e.filter_noalloc(q, F.ALGO_GSI, buf.data_ptr())
+        got = buf.cpu().numpy().reshape(3, V)
+        assert not got[1].any() and got[0].any()
+        assert np.array_equal(got, want)
+
+        # one label class of 2^21 + 64 vertices: a 32-vertex query needs more
+        # than 2^21 bitmap words
+        big = F.gen_rmat((1 << 21) + 64, 1 << 21, seed=13)
+        e.load_graph(big)
+        path = F.Query(np.zeros(32, np.int32), np.array([(i, i + 1) for i in range(31)], np.uint32))
+        sentinel = torch.full((64,), 0xAB, dtype=torch.uint8, device="cuda:0")
+        torch.cuda.synchronize()
+        with pytest.raises(F.FsigError) as ei:
+            e.filter_noalloc(path, F.ALGO_GSI, sentinel.data_ptr())
+        assert ei.value.status == F.EADMISSION
+        assert (sentinel.cpu().numpy() == 0xAB).all()
+
+        # the largest label table a loaded graph can have (4096 labels) fits;
+        # the engine refuses graphs with more labels when they are loaded
+        L = 4096
+        labels = np.arange(L, dtype=np.int32)
+        edges = np.array([(i, i + 1) for i in range(L - 1)], np.uint32)
+        e.load_graph(F.Graph(labels, edges))
+        q2 = F.Query(np.array([5, 6], np.int32), np.array([[0, 1]], np.uint32))
+        out = torch.full((2 * L,), 0xAB, dtype=torch.uint8, device="cuda:0")
+        torch.cuda.synchronize()
+        e.filter_noalloc(q2, F.ALGO_GSI, out.data_ptr())
+        flags = out.cpu().numpy().reshape(2, L)
+        assert np.array_equal(flags, e.filter(q2, F.ALGO_GSI, refine_iters=0))
+        assert flags[0, 5] == 1 and flags[1, 6] == 1 and flags.sum() == 2
+        with pytest.raises(F.FsigError) as ei:
+            e.load_graph(F.Graph(np.arange(L + 1, dtype=np.int32),
+                                 np.array([(i, i + 1) for i in range(L)], np.uint32)))
+        assert ei.value.status == F.EINVAL
