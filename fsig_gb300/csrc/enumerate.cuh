@@ -180,16 +180,20 @@ __global__ void __launch_bounds__(kEnumWarps * 32, kEnumMinBlocks) enumerate_ker
   // a query examines does not depend on how its work was split (ranges are
   // cut at multiples of 32 from the same origins), so whether it exceeds the
   // limit does not either.
+  // Also stops the warp's work (true) once the pass has recorded an error:
+  // the call will fail anyway, so it returns without finishing the pass.
   auto over_limit = [&]() -> bool {
-    if (!A.work_cap) return false;
     int stop = 0;
     if (lane == 0) {
-      if (pend) {
-        const unsigned long long tot = atomicAdd(&A.res[cur_q].work, (unsigned long long)pend) + pend;
-        pend = 0;
-        if (tot > A.work_cap) atomicExch(&A.res[cur_q].aborted, 1u);
+      if (A.work_cap) {
+        if (pend) {
+          const unsigned long long tot = atomicAdd(&A.res[cur_q].work, (unsigned long long)pend) + pend;
+          pend = 0;
+          if (tot > A.work_cap) atomicExch(&A.res[cur_q].aborted, 1u);
+        }
+        stop = *(volatile unsigned int*)&A.res[cur_q].aborted != 0;
       }
-      stop = *(volatile unsigned int*)&A.res[cur_q].aborted != 0;
+      stop |= *(volatile uint32_t*)&A.ctr[3 * kCtrStride] != 0;
     }
     return __shfl_sync(kFull, stop, 0) != 0;
   };
@@ -560,7 +564,7 @@ __global__ void __launch_bounds__(kEnumWarps * 32, kEnumMinBlocks) enumerate_ker
       }
       return;
     }
-    if (A.work_cap && over_limit()) return;
+    if (over_limit()) return;
     const uint32_t t_start = uint32_t(clock());
     uint32_t lv = d;
     enter(d, lo_set, hi_set);
@@ -620,7 +624,7 @@ __global__ void __launch_bounds__(kEnumWarps * 32, kEnumMinBlocks) enumerate_ker
   };
 
   for (;;) {
-    // 1. input tasks
+    // 1. input tasks (after an error every task returns at once: over_limit)
     uint32_t t0 = T_in;
     if (lane == 0 && *(volatile uint32_t*)&A.ctr[0 * kCtrStride] < T_in) t0 = atomicAdd(&A.ctr[0 * kCtrStride], A.chunk);
     t0 = __shfl_sync(kFull, t0, 0);
@@ -676,7 +680,7 @@ __global__ void __launch_bounds__(kEnumWarps * 32, kEnumMinBlocks) enumerate_ker
         if (*(volatile uint32_t*)&A.ctr[5 * kCtrStride] == 0 &&
             *(volatile uint32_t*)&A.ctr[2 * kCtrStride] >= min(*(volatile uint32_t*)&A.ctr[1 * kCtrStride], A.out_cap))
           break;
-        if (global_ns() - t_idle >= idle_ns) break;
+        if (global_ns() - t_idle >= idle_ns || *(volatile uint32_t*)&A.ctr[3 * kCtrStride]) break;
         __nanosleep(sleep_ns);
         if (sleep_ns < 8192) sleep_ns <<= 1;
       }

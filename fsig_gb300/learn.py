@@ -140,6 +140,49 @@ def alternative_orders(q: Query, cand, k: int, rng: np.random.Generator, around=
     return out
 
 
+def gsi_completion(prefix, masks, cand) -> list:
+    """The order that starts with `prefix` and continues by the heuristic
+    order's rule (match/GSI.cu:105-149): the frontier vertex of lowest score,
+    a score being the candidate count times 0.9 per placed neighbour (lowest
+    id on ties)."""
+    n = len(masks)
+    score = [float(c) for c in cand]
+    placed, order = 0, []
+
+    def place(u):
+        nonlocal placed
+        order.append(int(u))
+        placed |= 1 << int(u)
+        for w in range(n):
+            if (masks[u] >> w) & 1 and not (placed >> w) & 1:
+                score[w] *= 0.9
+
+    for u in prefix:
+        place(u)
+    while len(order) < n:
+        best = -1
+        for u in range(n):
+            if (placed >> u) & 1 or not (masks[u] & placed):
+                continue
+            if best < 0 or score[u] < score[best]:
+                best = u
+        place(best)
+    return order
+
+
+def prefix_orders(q: Query, cand, depth: int = 2) -> list:
+    """Every connected order prefix of `depth` vertices, each completed by the
+    heuristic rule (gsi_completion): an exhaustive search over the first
+    positions, where the choice matters most."""
+    masks = [int(x) for x in adjacency_masks(q)]
+    n = q.num_vertices
+    prefixes = [[u] for u in range(n)]
+    for _ in range(min(depth, n) - 1):
+        prefixes = [p + [w] for p in prefixes for w in range(n)
+                    if w not in p and any((masks[u] >> w) & 1 for u in p)]
+    return [gsi_completion(p, masks, cand) for p in prefixes]
+
+
 @dataclasses.dataclass
 class QueryLog:
     query: Query
@@ -166,12 +209,15 @@ class QueryLog:
 
 
 def collect_logs(engine: Engine, queries: Sequence[Query], algo: int = ALGO_FUSED, per_query: int = 16,
-                 seed: int = 0, batch: int = 2048, heuristic_limit: int = 0) -> list:
+                 seed: int = 0, batch: int = 2048, heuristic_limit: int = 0, prefix_depth: int = 0) -> list:
     """Order/cost logs for the queries on the engine's resident graph.
     Queries whose heuristic run exceeds heuristic_limit (0: none) are dropped.
-    Alternatives run in batches that share one work limit, the largest
-    heuristic work among their queries; an alternative costlier than its own
-    query's heuristic is recorded as aborted."""
+    The alternatives are `per_query` sampled orders (alternative_orders), or
+    with prefix_depth > 0 every order prefix of that many vertices completed
+    by the heuristic rule (prefix_orders).  Alternatives run in batches that
+    share one work limit, the largest heuristic work among their queries; an
+    alternative costlier than its own query's heuristic is recorded as
+    aborted."""
     rng = np.random.default_rng(seed)
     logs = []
     limit = heuristic_limit or UNCAPPED
@@ -184,7 +230,13 @@ def collect_logs(engine: Engine, queries: Sequence[Query], algo: int = ALGO_FUSE
                 continue
             lg = QueryLog(q, list(r.candidates), r.count, r.hash, list(r.order), int(r.work), [], [], [], 0)
             logs.append(lg)
-            for o in alternative_orders(q, r.candidates, per_query, rng, around=lg.heuristic_order):
+            cands = (prefix_orders(q, r.candidates, prefix_depth) if prefix_depth > 0 else
+                     alternative_orders(q, r.candidates, per_query, rng, around=lg.heuristic_order))
+            seen = {tuple(lg.heuristic_order)}
+            for o in cands:
+                if tuple(o) in seen:
+                    continue
+                seen.add(tuple(o))
                 alts.append((Query(q.labels, q.edges, order=np.asarray(o, np.uint32)), lg))
         # sort by the owner's work so each batch's shared limit stays close to its members'
         alts.sort(key=lambda t: t[1].heuristic_work)

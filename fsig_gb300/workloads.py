@@ -26,10 +26,11 @@ GPU engine; it is made once and written to a manifest
 (fsig_gb300/manifests/<name>.json) that lists, in batch order, each query's
 generator spec (vertices, walk mode, seed, label floor) with the work and
 embedding count and set hash measured then, and for every batch the fixed
-subset of its queries that the CPU reference arm times.  ``load(name)`` rebuilds the graph
-and the queries from the manifest with the host generators alone, and checks
-the graph's digest, so both benchmark arms and the tests run the same queries
-without opening the engine.
+subset of its queries that the CPU reference arm times (the first queries in
+batch order until their work adds up to REF_WORK).  ``load(name)`` rebuilds
+the graph and the queries from the manifest with the host generators alone,
+and checks the graph's digest, so both benchmark arms and the tests run the
+same queries without opening the engine.
 
     python -m fsig_gb300.workloads --write c5 c4 c2 c1 --out DIR   (on a GPU machine)
 """
@@ -239,7 +240,11 @@ def _ref_subset(work, target_work: int, per_query_work: int):
     return idx
 
 
-def make_manifest(engine, name: str, ref_work: int = 1 << 25, ref_query_work: int = 1 << 23) -> dict:
+REF_WORK = 1 << 26          # per batch: the CPU arm's sample adds up to about this much work
+REF_QUERY_WORK = 1 << 26    # ... from queries of at most this much work each (all of a workload's)
+
+
+def make_manifest(engine, name: str, ref_work: int = REF_WORK, ref_query_work: int = REF_QUERY_WORK) -> dict:
     t = time.time()
     g = build_graph(name)
     csr = g.csr()

@@ -4,6 +4,7 @@
 #include "oracle.h"
 
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <cstdio>
 #include <cstring>
@@ -503,22 +504,47 @@ int orc_match(uint32_t V, const int32_t* labels, const uint32_t* off, const uint
       ord[i] = order[i];
     }
   } else {
-    // Default: start at the highest-degree query vertex, then repeatedly take
-    // the unplaced vertex with the most placed neighbours (lowest id on ties).
-    uint32_t placed = 0, first = 0;
-    for (uint32_t u = 1; u < n; u++) if (qdeg[u] > qdeg[first]) first = u;
-    ord[0] = first;
-    placed |= 1u << first;
-    for (uint32_t i = 1; i < n; i++) {
-      int bestc = -1;
-      uint32_t bu = 0;
+    // Default: the rule of GSI::generate_join_order (match/GSI.cu:105-149)
+    // over candidate counts from the label and degree test: the vertex with
+    // the fewest candidates first, then repeatedly the unplaced neighbour of
+    // the placed ones with the lowest score, a vertex's score shrinking by
+    // 0.9 for every placed neighbour (lowest id on ties).  Any order gives the
+    // same count and hash; this one keeps the search small.
+    std::vector<uint32_t> qlab_idx(n);
+    std::vector<int32_t> distinct;
+    for (uint32_t u = 0; u < n; u++) {
+      auto it = std::find(distinct.begin(), distinct.end(), qlabels[u]);
+      qlab_idx[u] = uint32_t(it - distinct.begin());
+      if (it == distinct.end()) distinct.push_back(qlabels[u]);
+    }
+    // hist[k][d]: data vertices of the k-th query label with degree d (d capped at 32)
+    std::vector<std::array<uint64_t, 33>> hist(distinct.size());
+    for (auto& h : hist) h.fill(0);
+    for (uint32_t v = 0; v < V; v++) {
+      auto it = std::find(distinct.begin(), distinct.end(), labels[v]);
+      if (it == distinct.end()) continue;
+      const uint32_t d = std::min<uint32_t>(off[v + 1] - off[v], 32u);
+      hist[size_t(it - distinct.begin())][d]++;
+    }
+    std::vector<double> score(n);
+    for (uint32_t u = 0; u < n; u++) {
+      uint64_t cnt = 0;
+      for (uint32_t d = std::min<uint32_t>(qdeg[u], 32u); d <= 32; d++) cnt += hist[qlab_idx[u]][d];
+      score[u] = double(cnt);
+    }
+    uint32_t placed = 0;
+    for (uint32_t i = 0; i < n; i++) {
+      uint32_t bu = n;
       for (uint32_t u = 0; u < n; u++) {
         if ((placed >> u) & 1u) continue;
-        int c = __builtin_popcount(qadj[u] & placed);
-        if (c > bestc) { bestc = c; bu = u; }
+        if (i > 0 && !(qadj[u] & placed)) continue;
+        if (bu == n || score[u] < score[bu]) bu = u;
       }
+      if (bu == n) return -4;  // disconnected query
       ord[i] = bu;
       placed |= 1u << bu;
+      for (uint32_t w = 0; w < n; w++)
+        if (((qadj[bu] >> w) & 1u) && !((placed >> w) & 1u)) score[w] *= 0.9;
     }
   }
   MatchCtx c;

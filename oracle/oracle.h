@@ -72,8 +72,9 @@ void orc_refine(uint32_t V, const int32_t* labels, const uint32_t* offsets, cons
 
 // ---- matcher ----
 // Counts injective label-preserving embeddings of the query (n <= 32 vertices,
-// m undirected edges qedges[2m]) into the simple data graph.  order may be null
-// (a default connected order is used).  level_counts (may be null) receives, per
+// m undirected edges qedges[2m]) into the simple data graph.  order may be null:
+// then the order follows GSI::generate_join_order (match/GSI.cu:105-149) over
+// label-and-degree candidate counts (results never depend on the order).  level_counts (may be null) receives, per
 // depth d in [0,n), the number of partial embeddings of length d+1.
 // Returns 0 on success, negative on bad input.
 int orc_match(uint32_t V, const int32_t* labels, const uint32_t* offsets, const uint32_t* edges,
