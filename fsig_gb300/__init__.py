@@ -56,7 +56,8 @@ class _BatchOpts(C.Structure):
     _fields_ = [("algo", C.c_int), ("order_source", C.c_int), ("refine_iters", C.c_int), ("use_graph", C.c_int),
                 ("chunk", C.c_uint32), ("split_len", C.c_uint32), ("split_cycles", C.c_uint64),
                 ("max_work", C.c_uint64), ("warps_per_block", C.c_uint32), ("learned_window", C.c_uint32),
-                ("no_classes", C.c_uint32), ("isect", C.c_uint32), ("refine_coop", C.c_uint32)]
+                ("no_classes", C.c_uint32), ("isect", C.c_uint32), ("refine_coop", C.c_uint32),
+                ("learned_prefix", C.c_uint32)]
 
 
 class _Stats(C.Structure):
@@ -510,11 +511,13 @@ class Engine:
     def match_batch(self, qs: Sequence[Query], algo: int = ALGO_FUSED, order_source: int = ORDER_HEURISTIC,
                     refine_iters: int = -1, chunk: int = 0, use_graph: bool = False, split_len: int = 0,
                     split_cycles: int = 0, max_work: int = 0, warps_per_block: int = 0,
-                    learned_window: int = 0, classes: bool = True, isect: int = 0, refine_coop: int = 0) -> list:
+                    learned_window: int = 0, classes: bool = True, isect: int = 0, refine_coop: int = 0,
+                    learned_prefix: int = 0) -> list:
         arr, keep = _pack_queries(qs)
         res = (_Result * max(len(qs), 1))()
         opts = _BatchOpts(algo, order_source, refine_iters, 1 if use_graph else 0, chunk, split_len, split_cycles,
-                          max_work, warps_per_block, learned_window, 0 if classes else 1, isect, refine_coop)
+                          max_work, warps_per_block, learned_window, 0 if classes else 1, isect, refine_coop,
+                          learned_prefix)
         self._check(self._L.fsig_match_batch(self._h, len(qs), arr, C.byref(opts), res), "match_batch")
         return [_result(res[i]) for i in range(len(qs))]
 

@@ -14,7 +14,9 @@ The enumeration kernel's behaviour on a workload depends on five knobs of
   adaptive (the 32 entries after a segment's cursor first, merge-like, then a
   warp-cooperative 32-ary window search, shuffle search of windows of <= 32
   entries and per-lane binary search of longer ones), 1 window search only
-  (galloping-like), 2 per-lane binary search of the whole segment.
+  (galloping-like), 2 per-lane binary search of the whole segment, 3 the
+  tile search for segments whose rest fits 32 entries and per-lane binary
+  search for longer ones.
 
 When the batch refines candidates (``refine_iters`` > 0) one more joins:
 
@@ -48,7 +50,7 @@ GRID = {
     "chunk": [1, 2, 4, 8],
     "split_len": [64, 128, 256, 512, 1024],
     "split_cycles": [1000, 4000, 16000, 64000],
-    "isect": [0, 1, 2],
+    "isect": [0, 1, 2, 3],
 }
 DEFAULTS = {"warps_per_block": 8, "chunk": 1, "split_len": 256, "split_cycles": 4000, "isect": 0}
 REFINE_GRID = {"refine_coop": [8, 32, 128, 0xFFFFFFFF]}

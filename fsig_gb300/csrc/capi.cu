@@ -380,7 +380,7 @@ int fsig_match_batch(fsig_engine* h, uint32_t nq, const fsig_query* qs, const fs
   int rc = select(h);
   if (rc) return finish(h, rc);
   if ((nq && (!qs || !out))) return finish(h, fsig::fail(FSIG_EINVAL, "null argument"));
-  fsig_batch_opts def{FSIG_ALGO_FUSED, FSIG_ORDER_HEURISTIC, -1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  fsig_batch_opts def{FSIG_ALGO_FUSED, FSIG_ORDER_HEURISTIC, -1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   const fsig_batch_opts& bo = opts ? *opts : def;
   if (bo.algo != FSIG_ALGO_FSIG && bo.algo != FSIG_ALGO_GSI && bo.algo != FSIG_ALGO_FUSED)
     return finish(h, fsig::fail(FSIG_EINVAL, "unknown algorithm"));
@@ -406,6 +406,7 @@ int fsig_match_batch(fsig_engine* h, uint32_t nq, const fsig_query* qs, const fs
   o.use_graph = bo.use_graph != 0;
   o.classes = bo.no_classes == 0;
   if (bo.learned_window) o.learned_window = bo.learned_window;
+  if (bo.learned_prefix) o.learned_prefix = std::min<uint32_t>(bo.learned_prefix, 32u);
   if (bo.warps_per_block) {
     if (bo.warps_per_block > fsig::kEnumWarps) return finish(h, fsig::fail(FSIG_EINVAL, "warps_per_block too large"));
     o.warps_per_block = bo.warps_per_block;
@@ -414,7 +415,7 @@ int fsig_match_batch(fsig_engine* h, uint32_t nq, const fsig_query* qs, const fs
   if (bo.split_len) o.split = bo.split_len;
   if (bo.split_cycles) o.budget_cycles = (long long)bo.split_cycles;
   o.max_work = bo.max_work;
-  if (bo.isect > 2) return finish(h, fsig::fail(FSIG_EINVAL, "unknown intersection strategy"));
+  if (bo.isect > 3) return finish(h, fsig::fail(FSIG_EINVAL, "unknown intersection strategy"));
   o.isect = bo.isect;
   if (bo.refine_coop) o.refine_coop = bo.refine_coop;
   fsig::BatchOutput out_b;

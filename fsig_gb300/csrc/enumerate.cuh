@@ -92,6 +92,7 @@ struct EnumArgs {
 constexpr uint32_t kIsectAdaptive = 0;  // the 32 entries after the cursor first (merge-like), else window search
 constexpr uint32_t kIsectSearch = 1;    // 32-ary window search from the cursor (galloping-like)
 constexpr uint32_t kIsectBinary = 2;    // every lane binary-searches the rest of the segment alone
+constexpr uint32_t kIsectHybrid = 3;    // the tile when the segment's rest fits 32 entries, else as kIsectBinary
 
 constexpr uint32_t kErrTimeout = 1u;
 constexpr uint32_t kCtrStride = 32;        // one 128-byte line per counter
@@ -258,14 +259,14 @@ __global__ void __launch_bounds__(kEnumWarps * 32, kEnumMinBlocks) enumerate_ker
       const uint32_t j = __ffs(bw) - 1;
       bw &= bw - 1;
       const uint32_t lo = __shfl_sync(kFull, seg_lo, j), hi = __shfl_sync(kFull, seg_hi, j);
-      if (A.isect == kIsectBinary) {
+      if (A.isect == kIsectBinary || (A.isect == kIsectHybrid && hi - lo > 32)) {
         // no cooperation and no cursor: each surviving lane searches alone
         if (pred) pred = bsearch_range(g.adj, lo, hi, x, bytes);
         if (__ballot_sync(kFull, pred) == 0) break;
         continue;
       }
       uint32_t v = 0xffffffffu, ta = 0, tb = 32;
-      if (A.isect == kIsectAdaptive) {
+      if (A.isect != kIsectSearch) {
         const uint32_t idx = lo + lane;
         v = idx < hi ? __ldg(g.adj + idx) : 0xffffffffu;
         if (idx < hi) bytes += 4;
@@ -273,7 +274,7 @@ __global__ void __launch_bounds__(kEnumWarps * 32, kEnumMinBlocks) enumerate_ker
         tb = __popc(__ballot_sync(kFull, v <= xlast));
       }
       uint32_t a, b;
-      if (A.isect == kIsectAdaptive && (tb < 32 || lo + 32 >= hi)) {
+      if (A.isect != kIsectSearch && (tb < 32 || lo + 32 >= hi)) {
         // window [lo + ta, lo + tb) lies in this tile: shuffle search
         b = lo + tb;
         uint32_t l2 = ta, h2 = tb;

@@ -299,10 +299,13 @@ __device__ __forceinline__ uint32_t warp_argmin(float s, uint32_t id) {
   return id;
 }
 
+// With scores (kOrderScores), the first `lprefix` positions are chosen by the
+// scores and the rest by the GSI rule from that prefix on (candidate count,
+// times 0.9 per placed neighbour, the prefix's vertices included).
 __global__ void order_kernel(const QVert* __restrict__ qv, const uint32_t* __restrict__ qoff, uint32_t Q,
                              const uint32_t* __restrict__ counts, uint32_t mode, const float* __restrict__ scores,
                              const uint32_t* __restrict__ given, Plan* plans, uint32_t* root_count,
-                             uint32_t* orders_out) {
+                             uint32_t* orders_out, uint32_t lprefix = kMaxQ) {
   const uint32_t lane = threadIdx.x & 31;
   for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < Q; q += (gridDim.x * blockDim.x) >> 5) {
     const uint32_t g0 = qoff[q], n = qoff[q + 1] - g0;
@@ -316,6 +319,7 @@ __global__ void order_kernel(const QVert* __restrict__ qv, const uint32_t* __res
     const bool ok = n > 0 && __ballot_sync(kFull, live && cnt == 0) == 0;
 
     float score = float(cnt);
+    float gscore = float(cnt);   // GSI-rule score that continues a scored prefix
     uint32_t root_only = kFull;  // position 0 restricted to this vertex when != kFull
     if (mode == kOrderMMatch) {
       // 2-core by peeling vertices of degree <= 1 (match/MMatch.cu:543-607)
@@ -368,11 +372,13 @@ __global__ void order_kernel(const QVert* __restrict__ qv, const uint32_t* __res
         bool elig = live && !((placed >> lane) & 1u);
         if (i == 0) elig = elig && (root_only == kFull || lane == root_only);
         else elig = elig && (adj & placed) != 0;
-        const uint32_t u = warp_argmin(elig ? score : INFINITY, elig ? lane : 0xffffu);
+        const float sc = (mode == kOrderScores && i >= lprefix) ? gscore : score;
+        const uint32_t u = warp_argmin(elig ? sc : INFINITY, elig ? lane : 0xffffu);
         if (u >= n) break;  // cannot happen for connected queries
         placed |= 1u << u;
         if (lane == i) myord = u;
         if (mode == kOrderGSI && live && ((adj >> u) & 1u)) score = float(double(score) * 0.9);
+        if (mode == kOrderScores && live && ((adj >> u) & 1u)) gscore = float(double(gscore) * 0.9);
       }
     }
     // Plan for position i = lane.
@@ -1073,7 +1079,7 @@ int run_batch(Engine& e, const std::vector<HostQuery>& qs, const BatchOptions& o
       return fail(FSIG_EADMISSION, "root list does not fit the device arena");
     FSIG_CUDA_TRY(cudaMemsetAsync(d_rootcnt, 0, sizeof(uint32_t) * (uint64_t(Q) + 1), s));
     order_kernel<<<(Q + 7) / 8, 256, 0, s>>>(d_qv, d_qoff, Q, d_counts, order_mode, d_score_src, d_given, d_plans,
-                                             d_rootcnt, d_orders);
+                                             d_rootcnt, d_orders, opt.learned ? opt.learned_prefix : kMaxQ);
     FSIG_CUDA_TRY(cudaGetLastError());
     rc = device_exclusive_scan<uint32_t>(e.arena, d_rootcnt, d_rootoff, uint64_t(Q) + 1, nullptr, s, &launches);
     if (rc) return rc;

@@ -102,6 +102,7 @@ struct BatchOptions {
   const float* scores = nullptr;  // host scores per query vertex (kOrderScores), batch order
   bool learned = false;           // score with the loaded order network (kOrderScores)
   uint32_t learned_window = 32;   // positions a vertex may move from the heuristic order (32: any)
+  uint32_t learned_prefix = 32;   // positions chosen by the network; the rest by the GSI rule (32: all)
   // Refinement classes (refine_classes), when refine_iters > 0: members
   // share one bitmap, a vertex needs as many data neighbours in a query
   // neighbour class as it has query neighbours there, and dominated classes

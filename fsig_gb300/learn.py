@@ -372,26 +372,22 @@ def match_learned(engine: Engine, queries: Sequence[Query], algo: int = ALGO_FUS
 # training the packaged network: logs on the mid-scale graphs
 # ---------------------------------------------------------------------------
 def training_workloads():
-    """(name, graph builder, query specs, work limit) of the logs the packaged
-    network is trained on: the 320k-vertex Chung-Lu graph (exponent 2.1,
-    seed 2, 16 Zipf labels; the graph of the 8-vertex and the batched-serving
-    workloads) with 8-vertex and 4-32-vertex dense and sparse random-walk
-    queries and 12-32-vertex dense ones, all on labels >= 4.  Query seeds start at 70,000,000, apart from the
-    ones the benchmark draws.  The unlabeled 2^20-vertex R-MAT graph is not
-    logged: none of 64 of its 5-vertex queries examines fewer than 2^26 driver
-    entries, and every logged alternative order would cost as much again."""
-    from . import QUERY_DENSE, QUERY_SPARSE, gen_chung_lu, gen_labels
-
-    def chung_lu():
-        lab = gen_labels(320000, 16, "zipf", seed=2)
-        return gen_chung_lu(320000, 1050000, 2.1, seed=2, labels=lab)
-
-    rng = np.random.default_rng(70)
-    mixed = [(int(n), QUERY_DENSE if i % 2 else QUERY_SPARSE, 70_000_000 + i, 4)
-             for i, n in enumerate(rng.integers(4, 33, 3000))]
-    eight = [(8, QUERY_DENSE if i % 2 else QUERY_SPARSE, 71_000_000 + i, 4) for i in range(600)]
-    dense = [(int(n), QUERY_DENSE, 73_000_000 + i, 4) for i, n in enumerate(rng.integers(12, 33, 3000))]
-    return [("chung-lu 320k", chung_lu, mixed + eight + dense, 1 << 25)]
+    """(name, graph builder, query specs, work limit, queries kept) of the logs
+    the packaged network is trained on: the two graphs of the benchmarked
+    serving workloads with queries of their shapes drawn from seeds apart from
+    the benchmark's (workloads.candidate_specs of ranks 40 and 41; the
+    benchmark's manifests use rank 0): the 2^22-vertex Chung-Lu graph with
+    12-32-vertex dense walks on labels >= 8, and the 320k-vertex Chung-Lu graph
+    with 4-32-vertex dense and sparse walks on labels >= 4.  Only queries whose
+    heuristic run stays within the benchmark's selection budget are kept.  The
+    unlabeled 2^20-vertex R-MAT graph is not logged: its 5-vertex patterns
+    have about 1e15 embeddings each."""
+    from . import workloads as W
+    c5 = W.candidate_specs("c5", rank=40)[0][0][:8192]
+    dense, sparse = W.candidate_specs("c4", rank=41)[0]
+    c4 = [x for pair in zip(dense[:4096], sparse[:4096]) for x in pair]
+    return [("config-5 graph", lambda: W.build_graph("c5"), c5, W.WORK_BUDGET, 1024),
+            ("config-4 graph", lambda: W.build_graph("c4"), c4, W.WORK_BUDGET, 1024)]
 
 
 def main(argv=None):
@@ -401,7 +397,11 @@ def main(argv=None):
     from . import gen_queries, select_within_budget
     ap = argparse.ArgumentParser(description="Train the order-scoring network on the engine's own logs.")
     ap.add_argument("--out", default=str(WEIGHTS))
+    ap.add_argument("--prefix-depth", type=int, default=2,
+                    help="alternatives: every order prefix of this many vertices completed by the heuristic rule "
+                         "(0: --per-query sampled orders instead)")
     ap.add_argument("--per-query", type=int, default=16)
+    ap.add_argument("--queries", type=int, default=0, help="queries logged per workload (default: per workload)")
     ap.add_argument("--epochs", type=int, default=60)
     ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--work-limit", type=int, default=0,
@@ -414,14 +414,20 @@ def main(argv=None):
     logs = []
     with Engine(args.device, arena_bytes=48 << 30) as e:
         t0 = time.time()
-        for name, build, specs, limit in training_workloads():
+        for name, build, specs, limit, keep in training_workloads():
             g = build()
             csr = g.csr()
             e.load_graph(g)
-            qs = select_within_budget(e, gen_queries(g, specs, csr=csr), len(specs), args.work_limit or limit)
-            print(f"[learn] {name}: {len(qs)} of {len(specs)} queries within the work limit, "
-                  f"{time.time() - t0:.1f}s", flush=True)
-            lg = collect_logs(e, qs, per_query=args.per_query, seed=args.seed)
+            want = args.queries or keep
+            qs = []
+            for i in range(0, len(specs), 2048):
+                qs += select_within_budget(e, gen_queries(g, specs[i:i + 2048], csr=csr), want - len(qs),
+                                           args.work_limit or limit)
+                if len(qs) >= want:
+                    break
+            print(f"[learn] {name}: {len(qs)} queries within the work limit, {time.time() - t0:.1f}s", flush=True)
+            lg = collect_logs(e, qs, per_query=args.per_query, seed=args.seed, prefix_depth=args.prefix_depth,
+                              batch=1024)
             gain = sum(x.heuristic_work for x in lg) / max(sum(x.best[1] for x in lg), 1)
             print(f"[learn] {name}: {len(lg)} queries logged, best/heuristic total work 1/{gain:.3f}, "
                   f"{time.time() - t0:.1f}s", flush=True)

@@ -106,12 +106,18 @@ typedef struct {
                                segment's cursor first (merge-like), else a
                                warp-cooperative 32-ary window search; 1 window
                                search only (galloping-like); 2 every lane
-                               binary-searches the segment alone            */
+                               binary-searches the segment alone; 3 the
+                               tile search when the segment's rest fits 32
+                               entries, else as 2                           */
   uint32_t refine_coop;     /* refinement: a candidate's neighbour segment
                                longer than this is scanned by the whole warp
                                (warp per candidate), shorter ones by the
                                candidate's own lane (0: default 32;
                                0xffffffff: always a lane)                    */
+  uint32_t learned_prefix;  /* FSIG_ORDER_LEARNED: the network chooses the first
+                               this many positions, the heuristic rule (GSI's:
+                               candidate count, 0.9 per placed neighbour)
+                               continues from them (0: all positions)        */
 } fsig_batch_opts;
 
 /* ---- engine lifetime; replaces GPUSubgraphMatcher::init_GPU (match/subgraph_match.h:51-80)

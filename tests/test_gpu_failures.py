@@ -33,7 +33,9 @@ def path_query(n):
 def test_oversize_batch_is_refused_then_engine_recovers():
     g = F.gen_rmat(1 << 14, 1 << 17, 0.57, 0.19, 0.19, seed=21)
     off, adj = g.csr()
-    small = [pattern("c5"), path_query(3), pattern("k4_pendant")]
+    # small enough for the oracle (a few million embeddings at most)
+    triangle = F.Query(np.zeros(3, np.int32), np.array([[0, 1], [1, 2], [2, 0]], np.uint32))
+    small = [triangle, path_query(3), path_query(2)]
     # 512 MiB: the graph store and one small batch (work queues ~310 MiB)
     # fit; 4,000 queries of 32 vertices need ~0.8 GiB of root lists alone
     with F.Engine(0, arena_bytes=512 << 20) as e:
