@@ -520,7 +520,8 @@ def run_c3(args, dist):
                 name = names[k % len(names)]
                 q = W.pattern(name)
                 _, T = e.match_range(q, F.ALGO_GSI, 0, 0)
-                K = max(1, min(args.c3_strata, T))
+                # warm-up steps sample a single stratum
+                K = max(1, min(args.c3_strata if k >= args.warmup else 1, T))
                 bounds = np.linspace(0, T, K + 1).astype(np.int64)
                 cnt_est = time_est = 0.0
                 s_cnt = s_work = 0

@@ -11,12 +11,11 @@ The enumeration kernel's behaviour on a workload depends on five knobs of
 * ``split_cycles`` - SM cycles a task runs before its unexplored frontier may
   be handed to idle warps;
 * ``isect`` - the set-intersection strategy of the membership tests: 0
-  adaptive (the 32 entries after a segment's cursor first, merge-like, then a
-  warp-cooperative 32-ary window search, shuffle search of windows of <= 32
-  entries and per-lane binary search of longer ones), 1 window search only
-  (galloping-like), 2 per-lane binary search of the whole segment, 3 the
-  tile search for segments whose rest fits 32 entries and per-lane binary
-  search for longer ones.
+  every lane binary-searches the segment alone, 1 warp-cooperative 32-ary
+  window search (galloping-like), 2 adaptive (the 32 entries after a
+  segment's cursor first, merge-like, then the window search), 3 the tile
+  search for segments whose rest fits 32 entries and per-lane binary search
+  for longer ones.
 
 When the batch refines candidates (``refine_iters`` > 0) one more joins:
 

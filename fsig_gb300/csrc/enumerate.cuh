@@ -89,9 +89,9 @@ struct EnumArgs {
 };
 
 // Membership of a window's entries in a backward segment:
-constexpr uint32_t kIsectAdaptive = 0;  // the 32 entries after the cursor first (merge-like), else window search
+constexpr uint32_t kIsectBinary = 0;    // every lane binary-searches the rest of the segment alone (default)
 constexpr uint32_t kIsectSearch = 1;    // 32-ary window search from the cursor (galloping-like)
-constexpr uint32_t kIsectBinary = 2;    // every lane binary-searches the rest of the segment alone
+constexpr uint32_t kIsectAdaptive = 2;  // the 32 entries after the cursor first (merge-like), else window search
 constexpr uint32_t kIsectHybrid = 3;    // the tile when the segment's rest fits 32 entries, else as kIsectBinary
 
 constexpr uint32_t kErrTimeout = 1u;
@@ -447,14 +447,16 @@ __global__ void __launch_bounds__(kEnumWarps * 32, kEnumMinBlocks) enumerate_ker
       seg_hi = s[1];
       bytes += 8;
     }
-    // Leaf: lane j of the same-label depths holds the position of f_j in the
-    // driver range (kInvalid when absent); the range has no repeated entry, so
-    // f_j can only be the entry at that position.
+    // Leaf ranges of more than two windows: lane j of the same-label depths
+    // holds the position of f_j in the driver range (kInvalid when absent); the
+    // range has no repeated entry, so f_j can only be the entry at that
+    // position.  Shorter ranges compare by shuffles, window by window.
     uint32_t same_pos = kInvalid;
     unsigned long long Sp = 0;
     uint64_t tq = 0;
+    const bool by_pos = leaf && de - dp > 2 * kChunk;
     if (leaf) {
-      if ((same >> lane) & 1u) {
+      if (by_pos && ((same >> lane) & 1u)) {
         uint32_t lo = dp, hi = de;
         while (lo < hi) {
           const uint32_t mid = (lo + hi) >> 1;
@@ -480,7 +482,7 @@ __global__ void __launch_bounds__(kEnumWarps * 32, kEnumMinBlocks) enumerate_ker
         pred = (__ldg(bm + (bit >> 5)) >> (bit & 31)) & 1u;
         bytes += 4;
       }
-      if (leaf) {
+      if (by_pos) {
         uint32_t hit = __ballot_sync(kFull, same_pos - dp < nvalid);
         while (hit) {
           const uint32_t j = __ffs(hit) - 1;

@@ -44,7 +44,9 @@ def test_filter_noalloc_absent_label_and_limits():
     torch = pytest.importorskip("torch")
     lab = F.gen_labels(4000, 6, "uniform", seed=12)
     g = F.gen_rmat(4000, 16000, seed=12, labels=lab)
-    q = F.Query(np.array([0, 999, 2], np.int32), np.array([[0, 1], [1, 2]], np.uint32))
+    # vertex 2's label 999 is absent (a vertex without bitmap words); vertex
+    # 0 (label 0, a neighbour of label 1) has candidates
+    q = F.Query(np.array([0, 1, 999], np.int32), np.array([[0, 1], [1, 2]], np.uint32))
     with F.Engine(0, arena_bytes=1 << 30) as e:
         e.load_graph(g)
         V = e.graph_info()["V"]
@@ -53,7 +55,7 @@ def test_filter_noalloc_absent_label_and_limits():
         torch.cuda.synchronize()
         e.filter_noalloc(q, F.ALGO_GSI, buf.data_ptr())
         got = buf.cpu().numpy().reshape(3, V)
-        assert not got[1].any() and got[0].any()
+        assert not got[2].any() and got[0].any()
         assert np.array_equal(got, want)
 
         # one label class of 2^21 + 64 vertices: a 32-vertex query needs more
