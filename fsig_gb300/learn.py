@@ -258,13 +258,40 @@ def collect_logs(engine: Engine, queries: Sequence[Query], algo: int = ALGO_FUSE
     return logs
 
 
-def training_set(engine: Engine, logs: Sequence[QueryLog], algo: int = ALGO_FUSED, margin: float | None = None):
-    """(node offsets, features, neighbour masks, targets) for the logs; with
-    margin, an alternative must be cheaper than margin x the heuristic's work
-    to become the target."""
+def cost_targets(lg: QueryLog) -> np.ndarray:
+    """Per query vertex u: log2 of (the least work found among the logged
+    orders that start with u) / (the heuristic order's work), clipped to
+    [-1, 0.5]; 0.5 when no order starting with u finished within the
+    heuristic's work.  Lower is a better first vertex, so ordering by the
+    lowest predicted value (FSIG_ORDER_LEARNED with learned_prefix) starts
+    where the search found the least work."""
+    n = lg.query.num_vertices
+    best = np.full(n, np.inf)
+    h = max(lg.heuristic_work, 1)
+    best[lg.heuristic_order[0]] = h
+    for o, w in zip(lg.orders, lg.works):
+        best[o[0]] = min(best[o[0]], max(w, 1))
+    t = np.where(np.isfinite(best), np.log2(np.where(np.isfinite(best), best, 1.0) / h), 0.5)
+    return np.clip(t, -1.0, 0.5).astype(np.float32)
+
+
+def training_set(engine: Engine, logs: Sequence[QueryLog], algo: int = ALGO_FUSED, margin: float | None = None,
+                 target: str = "position", oversample: int = 0):
+    """(node offsets, features, neighbour masks, targets) for the logs.
+    target "position": a vertex's position in the cheapest order found /
+    (n - 1), an alternative becoming the target only below margin x the
+    heuristic's work; "cost": cost_targets.  With oversample k, a query
+    whose cheapest order saves a fraction s of the heuristic's work appears
+    1 + round(k * s / 0.2) times."""
     if margin is not None:
         for lg in logs:
             lg.margin = margin
+    if oversample:
+        rep = []
+        for lg in logs:
+            saved = 1.0 - min([lg.heuristic_work] + lg.works) / max(lg.heuristic_work, 1)
+            rep += [lg] * (1 + int(round(oversample * max(saved, 0.0) / 0.2)))
+        logs = rep
     qs = [lg.query for lg in logs]
     feat = engine.mpnn_features(qs, [lg.candidates for lg in logs], algo)
     goff = np.zeros(len(qs) + 1, np.uint32)
@@ -272,11 +299,38 @@ def training_set(engine: Engine, logs: Sequence[QueryLog], algo: int = ALGO_FUSE
     nbr = np.concatenate([adjacency_masks(q) for q in qs]) if qs else np.zeros(0, np.uint32)
     tgt = np.zeros(int(goff[-1]), np.float32)
     for i, lg in enumerate(logs):
+        if target == "cost":
+            tgt[goff[i]:goff[i + 1]] = cost_targets(lg)
+            continue
         order, _ = lg.best
         n = len(order)
         for pos, u in enumerate(order):
             tgt[goff[i] + u] = pos / max(n - 1, 1)
     return goff, feat, nbr, tgt
+
+
+def save_logs(path, logs) -> None:
+    """(workload name, QueryLog) pairs as JSON (the data graph's workload,
+    query, candidates, heuristic order and work, the finished alternatives
+    and their work), to retrain without searching again."""
+    import json
+    rec = [dict(graph=name, labels=[int(x) for x in lg.query.labels], edges=np.asarray(lg.query.edges).reshape(-1).tolist(),
+                candidates=[int(x) for x in lg.candidates], count=int(lg.count), hash=str(int(lg.hash)),
+                heuristic_order=[int(x) for x in lg.heuristic_order], heuristic_work=int(lg.heuristic_work),
+                orders=lg.orders, works=[int(w) for w in lg.works], aborted=int(lg.aborted)) for name, lg in logs]
+    Path(path).write_text(json.dumps(rec))
+
+
+def load_logs(path) -> list:
+    """(workload name, QueryLog) pairs written by save_logs."""
+    import json
+    out = []
+    for r in json.loads(Path(path).read_text()):
+        q = Query(np.asarray(r["labels"], np.int32), np.asarray(r["edges"], np.uint32).reshape(-1, 2))
+        out.append((r["graph"], QueryLog(q, r["candidates"], r["count"], int(r["hash"]), r["heuristic_order"],
+                                         r["heuristic_work"], r["orders"], r["works"], [[] for _ in r["works"]],
+                                         r["aborted"])))
+    return out
 
 
 def _subset(goff, feat, nbr, tgt, idx):
@@ -386,8 +440,8 @@ def training_workloads():
     c5 = W.candidate_specs("c5", rank=40)[0][0][:8192]
     dense, sparse = W.candidate_specs("c4", rank=41)[0]
     c4 = [x for pair in zip(dense[:4096], sparse[:4096]) for x in pair]
-    return [("config-5 graph", lambda: W.build_graph("c5"), c5, W.WORK_BUDGET, 1024),
-            ("config-4 graph", lambda: W.build_graph("c4"), c4, W.WORK_BUDGET, 1024)]
+    return [("c5", lambda: W.build_graph("c5"), c5, W.WORK_BUDGET, 1024),
+            ("c4", lambda: W.build_graph("c4"), c4, W.WORK_BUDGET, 1024)]
 
 
 def main(argv=None):
@@ -402,6 +456,13 @@ def main(argv=None):
                          "(0: --per-query sampled orders instead)")
     ap.add_argument("--per-query", type=int, default=16)
     ap.add_argument("--queries", type=int, default=0, help="queries logged per workload (default: per workload)")
+    ap.add_argument("--target", default="cost", choices=["cost", "position"],
+                    help="cost: log work ratio of the best order starting at each vertex; position: its position "
+                         "in the cheapest order found")
+    ap.add_argument("--oversample", type=int, default=4,
+                    help="repeat queries by the share of work their best order saves (0: no repeats)")
+    ap.add_argument("--save-logs", default="", help="write the logs here (JSON)")
+    ap.add_argument("--logs", default="", help="train on these saved logs instead of logging again")
     ap.add_argument("--epochs", type=int, default=60)
     ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--work-limit", type=int, default=0,
@@ -412,9 +473,20 @@ def main(argv=None):
     ap.add_argument("--device", type=int, default=0)
     args = ap.parse_args(argv)
     logs = []
+    all_logs = []
     with Engine(args.device, arena_bytes=48 << 30) as e:
         t0 = time.time()
-        for name, build, specs, limit, keep in training_workloads():
+        if args.logs:
+            from . import workloads as W
+            # features come from the engine's candidate counts: each log's graph must be resident
+            by_graph = {}
+            for name, x in load_logs(args.logs):
+                by_graph.setdefault(name, []).append(x)
+            for name, part in by_graph.items():
+                e.load_graph(W.build_graph(name))
+                logs.append((part, training_set(e, part, margin=args.margin, target=args.target,
+                                                oversample=args.oversample)))
+        for name, build, specs, limit, keep in ([] if args.logs else training_workloads()):
             g = build()
             csr = g.csr()
             e.load_graph(g)
@@ -431,7 +503,11 @@ def main(argv=None):
             gain = sum(x.heuristic_work for x in lg) / max(sum(x.best[1] for x in lg), 1)
             print(f"[learn] {name}: {len(lg)} queries logged, best/heuristic total work 1/{gain:.3f}, "
                   f"{time.time() - t0:.1f}s", flush=True)
-            logs.append((lg, training_set(e, lg, margin=args.margin)))
+            all_logs += [(name, x) for x in lg]
+            logs.append((lg, training_set(e, lg, margin=args.margin, target=args.target,
+                                          oversample=args.oversample)))
+        if args.save_logs and all_logs:
+            save_logs(args.save_logs, all_logs)
         goff = np.zeros(1, np.uint32)
         feats, nbrs, tgts = [], [], []
         for _, (o, f, nb, t) in logs:
