@@ -24,12 +24,16 @@ When the batch refines candidates (``refine_iters`` > 0) one more joins:
   (coalesced, one ballot per 32 entries), shorter ones by the candidate's own
   lane.
 
-With ``order_source = ORDER_LEARNED`` another knob joins the grid:
+With ``order_source = ORDER_LEARNED`` two more knobs join the grid:
 
 * ``learned_window`` - positions a vertex may move away from the heuristic
-  order.  It changes the orders and with them the work; a query whose learned
-  order goes over ``max_work`` is run again in heuristic order (as serving
-  does), and that run's device time counts towards the trial.
+  order;
+* ``learned_prefix`` - positions the network chooses before the heuristic
+  rule takes over.
+
+Both change the orders and with them the work; a query whose learned order
+goes over ``max_work`` is run again in heuristic order (as serving does), and
+that run's device time counts towards the trial.
 
 ``tune`` runs coordinate descent over a small grid on a sample batch: one knob
 at a time, each value timed by device time (CUDA events of the engine) as the
@@ -54,8 +58,8 @@ GRID = {
 DEFAULTS = {"warps_per_block": 8, "chunk": 1, "split_len": 256, "split_cycles": 4000, "isect": 0}
 REFINE_GRID = {"refine_coop": [8, 32, 128, 0xFFFFFFFF]}
 REFINE_DEFAULTS = {"refine_coop": 32}
-LEARNED_GRID = {"learned_window": [1, 2, 4, 32]}
-LEARNED_DEFAULTS = {"learned_window": 32}
+LEARNED_GRID = {"learned_window": [1, 2, 4, 32], "learned_prefix": [1, 2, 32]}
+LEARNED_DEFAULTS = {"learned_window": 32, "learned_prefix": 32}
 
 
 def _device_ms(engine: Engine) -> float:

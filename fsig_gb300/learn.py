@@ -456,7 +456,7 @@ def main(argv=None):
                          "(0: --per-query sampled orders instead)")
     ap.add_argument("--per-query", type=int, default=16)
     ap.add_argument("--queries", type=int, default=0, help="queries logged per workload (default: per workload)")
-    ap.add_argument("--target", default="cost", choices=["cost", "position"],
+    ap.add_argument("--target", default="position", choices=["cost", "position"],
                     help="cost: log work ratio of the best order starting at each vertex; position: its position "
                          "in the cheapest order found")
     ap.add_argument("--oversample", type=int, default=4,
