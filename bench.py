@@ -65,9 +65,9 @@ PEAKS = ROOT / "MEASURED_PEAKS.json"
 FALLBACK_HBM_GBS = 6800.0
 
 # DRAM bytes (read + write) of one enumerate_kernel launch on a config-5
-# batch, from an ncu capture (profiles/enumerate_kernel_c5.md); its loads are
-# served from L2 at about 99 %.
-ENUM_TRAFFIC_BYTES_PER_LAUNCH = 286_300_000
+# batch, from an ncu capture (profiles/enumerate_kernel_c5.md: 626.2 MB/s over
+# 403.4 ms); its loads are served from L2 at about 99 %.
+ENUM_TRAFFIC_BYTES_PER_LAUNCH = 252_600_000
 
 
 def log(*a):
@@ -509,6 +509,8 @@ def run_c3(args, dist):
     of the stratum's size times its sample's mean per task)."""
     if dist.rank != 0:
         return None
+    if args.c3_full:
+        return run_c3_full(args, dist)
     g = W.build_graph("c3")
     rng = np.random.default_rng(33)
     names = list(W.PATTERNS)
@@ -562,6 +564,40 @@ def run_c3(args, dist):
         "patterns": per, "clocks": clk.summary()}
 
 
+def run_c3_full(args, dist):
+    """One config-3 pattern over its whole task space at full size, in
+    fsig_match_range pieces of c3_piece root tasks: the exact count and hash
+    when every piece finishes within c3_budget_s seconds, else the part done."""
+    g = W.build_graph("c3")
+    q = W.pattern(args.c3_full)
+    count = hsum = 0
+    dev_s = 0.0
+    with F.Engine(dist.local, arena_bytes=args.arena_gb << 30) as e:
+        e.load_graph(g)
+        _, T = e.match_range(q, F.ALGO_GSI, 0, 0)
+        t0 = time.perf_counter()
+        done = 0
+        with ClockSampler(dist.local) as clk:
+            while done < T and time.perf_counter() - t0 < args.c3_budget_s:
+                r, _ = e.match_range(q, F.ALGO_GSI, done, min(T, done + args.c3_piece))
+                st = e.last_stats()
+                dev_s += (st["ms_filter"] + st["ms_join"]) / 1e3
+                count += r.count
+                hsum = (hsum + r.hash) % (1 << 64)
+                done = min(T, done + args.c3_piece)
+                log(f"[c3] {args.c3_full}: tasks {done}/{T}, {count} embeddings, {time.perf_counter() - t0:.0f}s")
+        wall = time.perf_counter() - t0
+    complete = done >= T
+    return {"metric": "embeddings/s, one unlabeled 5-vertex pattern at full size, every root task",
+            "value": sig(count / dev_s) if dev_s else 0.0, "unit": "embeddings/s", "n_gpus": dist.world,
+            "higher_is_better": True, "dtype": "u32", "data": "synthetic (seeded generators; no dataset available)",
+            "config": {"workload": "c3", "graph": W.GRAPH_DESC["c3"], "pattern": args.c3_full,
+                       "edges": [list(x) for x in W.PATTERNS[args.c3_full]], "piece_tasks": args.c3_piece},
+            "complete": complete, "tasks_done": done, "tasks_total": T,
+            "count": count if complete else None, "hash": hex(hsum) if complete else None,
+            "count_so_far": count, "device_s": round(dev_s, 3), "wall_s": round(wall, 1), "clocks": clk.summary()}
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -571,6 +607,10 @@ def main():
     ap.add_argument("--workload", default="c5", choices=["c5", "c4", "c3", "c2", "c1"])
     ap.add_argument("--c3-strata", type=int, default=64, help="config 3: strata of each pattern's task space")
     ap.add_argument("--c3-tasks", type=int, default=4, help="config 3: root tasks sampled per stratum")
+    ap.add_argument("--c3-full", default="", choices=[""] + list(W.PATTERNS),
+                    help="config 3: enumerate this pattern over every root task instead of sampling")
+    ap.add_argument("--c3-piece", type=int, default=16384, help="config 3 --c3-full: root tasks per call")
+    ap.add_argument("--c3-budget-s", type=float, default=1800.0, help="config 3 --c3-full: time budget")
     ap.add_argument("--algo", default="fused", choices=["fsig", "gsi", "fused"])
     ap.add_argument("--order", default=None, choices=["heuristic", "learned"],
                     help="default: learned when the packaged network exists")
