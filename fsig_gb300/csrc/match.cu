@@ -74,7 +74,7 @@ __device__ __forceinline__ uint32_t warp_transpose32(uint32_t x, uint32_t lane) 
   return x;
 }
 
-__global__ void __launch_bounds__(kFilterWarps * 32, 4) filter_kernel(GraphView g, const QVert* __restrict__ qv,
+__global__ void __launch_bounds__(kFilterWarps * 32, 8) filter_kernel(GraphView g, const QVert* __restrict__ qv,
                                                                    const uint32_t* __restrict__ lab_gidx,
                                                                    const uint32_t* __restrict__ lab_begin,
                                                                    uint32_t mode, uint32_t* __restrict__ pool) {
