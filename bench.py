@@ -566,8 +566,10 @@ def run_c3(args, dist):
 
 def run_c3_full(args, dist):
     """One config-3 pattern over its whole task space at full size, in
-    fsig_match_range pieces of c3_piece root tasks: the exact count and hash
-    when every piece finishes within c3_budget_s seconds, else the part done."""
+    fsig_match_range pieces of root tasks -- one task first (the lowest ids
+    are R-MAT's hubs, the heaviest roots), the piece doubled while a piece
+    takes under 10 s, up to c3_piece: the exact count and hash when the whole
+    space finishes within c3_budget_s seconds, else the part done."""
     g = W.build_graph("c3")
     q = W.pattern(args.c3_full)
     count = hsum = 0
@@ -577,22 +579,26 @@ def run_c3_full(args, dist):
         _, T = e.match_range(q, F.ALGO_GSI, 0, 0)
         t0 = time.perf_counter()
         done = 0
+        piece = 1
         with ClockSampler(dist.local) as clk:
             while done < T and time.perf_counter() - t0 < args.c3_budget_s:
-                r, _ = e.match_range(q, F.ALGO_GSI, done, min(T, done + args.c3_piece))
+                r, _ = e.match_range(q, F.ALGO_GSI, done, min(T, done + piece))
                 st = e.last_stats()
-                dev_s += (st["ms_filter"] + st["ms_join"]) / 1e3
+                ms = st["ms_filter"] + st["ms_join"]
+                dev_s += ms / 1e3
                 count += r.count
                 hsum = (hsum + r.hash) % (1 << 64)
-                done = min(T, done + args.c3_piece)
-                log(f"[c3] {args.c3_full}: tasks {done}/{T}, {count} embeddings, {time.perf_counter() - t0:.0f}s")
+                done = min(T, done + piece)
+                log(f"[c3] {args.c3_full}: tasks {done}/{T} (piece {piece}, {ms / 1e3:.1f}s), {count} embeddings, "
+                    f"{time.perf_counter() - t0:.0f}s")
+                piece = min(args.c3_piece, piece * 2) if ms < 10e3 else max(1, piece // 2)
         wall = time.perf_counter() - t0
     complete = done >= T
     return {"metric": "embeddings/s, one unlabeled 5-vertex pattern at full size, every root task",
             "value": sig(count / dev_s) if dev_s else 0.0, "unit": "embeddings/s", "n_gpus": dist.world,
             "higher_is_better": True, "dtype": "u32", "data": "synthetic (seeded generators; no dataset available)",
             "config": {"workload": "c3", "graph": W.GRAPH_DESC["c3"], "pattern": args.c3_full,
-                       "edges": [list(x) for x in W.PATTERNS[args.c3_full]], "piece_tasks": args.c3_piece},
+                       "edges": [list(x) for x in W.PATTERNS[args.c3_full]], "max_piece_tasks": args.c3_piece},
             "complete": complete, "tasks_done": done, "tasks_total": T,
             "count": count if complete else None, "hash": hex(hsum) if complete else None,
             "count_so_far": count, "device_s": round(dev_s, 3), "wall_s": round(wall, 1), "clocks": clk.summary()}
