@@ -110,7 +110,7 @@ struct WarpSmem {
 };
 
 __device__ __forceinline__ bool bsearch_range(const uint32_t* __restrict__ a, uint32_t lo, uint32_t hi, uint32_t x,
-                                              unsigned long long& bytes) {
+                                              uint32_t& bytes) {
   while (lo < hi) {
     const uint32_t mid = (lo + hi) >> 1;
     const uint32_t y = __ldg(a + mid);
@@ -125,7 +125,7 @@ __device__ __forceinline__ bool bsearch_range(const uint32_t* __restrict__ a, ui
 // First index in [lo, hi) of sorted a[] with a[i] >= key (warp-uniform key
 // and range): 32 pivots per round, then one 32-entry tile.
 __device__ __forceinline__ uint32_t warp_lower_bound(const uint32_t* __restrict__ a, uint32_t lo, uint32_t hi,
-                                                     uint32_t key, uint32_t lane, unsigned long long& bytes) {
+                                                     uint32_t key, uint32_t lane, uint32_t& bytes) {
   while (hi - lo > 32) {
     const uint32_t step = (hi - lo + 31) >> 5;
     const uint32_t idx = lo + lane * step;
@@ -157,8 +157,10 @@ __global__ void __launch_bounds__(kEnumWarps * 32, kEnumMinBlocks) enumerate_ker
 
   // lane-distributed level state
   uint32_t f = 0, dpos = 0, dend = 0, drv = 0, cnt = 0, it = 0;
-  unsigned long long S = 0, lc = 0;
-  unsigned long long my_count = 0, my_hash = 0, bytes = 0;
+  unsigned long long S = 0, my_hash = 0;
+  // per-lane counters in 32 bits, drained into the 64-bit device totals
+  // before any lane's can reach 2^31 (drain, at every periodic check)
+  uint32_t lc = 0, my_count = 0, bytes = 0;
   uint32_t pend = 0;  // driver entries examined, not yet published to res.work (lane 0; flushed every 64 windows)
   // event counters (lane 0); a warp's share of one launch fits 32 bits
   uint32_t n_tasks = 0, n_pops = 0, n_handoffs = 0, n_recs = 0, n_examine = 0;
@@ -166,12 +168,12 @@ __global__ void __launch_bounds__(kEnumWarps * 32, kEnumMinBlocks) enumerate_ker
 
   auto flush = [&]() {
     if (cur_q == kInvalid) return;
-    const unsigned long long c = warp_sum(my_count), h = warp_sum(my_hash);
+    const unsigned long long c = warp_sum((unsigned long long)my_count), h = warp_sum(my_hash);
     if (lane == 0 && (c | h)) {
       atomicAdd(&A.res[cur_q].count, c);
       atomicAdd(&A.res[cur_q].hash, h);
     }
-    if (lane < ws.plan.n && lc) atomicAdd(&A.res[cur_q].levels[lane], lc);
+    if (lane < ws.plan.n && lc) atomicAdd(&A.res[cur_q].levels[lane], (unsigned long long)lc);
     my_count = my_hash = 0;
     lc = 0;
   };
@@ -184,6 +186,12 @@ __global__ void __launch_bounds__(kEnumWarps * 32, kEnumMinBlocks) enumerate_ker
   // Also stops the warp's work (true) once the pass has recorded an error:
   // the call will fail anyway, so it returns without finishing the pass.
   auto over_limit = [&]() -> bool {
+    if (__any_sync(kFull, (lc | my_count | bytes) >= (1u << 30))) {
+      flush();
+      const unsigned long long b = warp_sum((unsigned long long)bytes);
+      if (lane == 0) atomicAdd(A.algo_bytes, b);
+      bytes = 0;
+    }
     int stop = 0;
     if (lane == 0) {
       if (A.work_cap) {
@@ -212,6 +220,10 @@ __global__ void __launch_bounds__(kEnumWarps * 32, kEnumMinBlocks) enumerate_ker
   };
 
   // Driver of depth lv from the backward neighbours' rows; stored in lane lv.
+  // Backward segment bounds loaded by the last enter(), kept for the scan
+  // that follows it at the same depth (lane j: segment j; c_lv: that depth).
+  uint32_t c_lo = 0, c_hi = 0, c_lv = kInvalid;
+
   auto enter = [&](uint32_t lv, uint32_t lo_set, uint32_t hi_set) {
     const uint32_t bw = ws.plan.bwd[lv];
     const int32_t lab = ws.plan.lab[lv];
@@ -223,6 +235,9 @@ __global__ void __launch_bounds__(kEnumWarps * 32, kEnumMinBlocks) enumerate_ker
       len = hi - lo;
       bytes += 8;
     }
+    c_lo = lo;
+    c_hi = hi;
+    c_lv = lv;
     const bool empty = __ballot_sync(kFull, len == 0) != 0;
     // shortest segment, lowest lane on ties: one warp reduction of (length, lane)
     const uint32_t key = len == kInvalid ? 0xffffffffu : (min(len, (1u << 27) - 1u) << 5) | lane;
@@ -440,13 +455,16 @@ __global__ void __launch_bounds__(kEnumWarps * 32, kEnumMinBlocks) enumerate_ker
     const uint32_t* __restrict__ bm = A.pool + ws.plan.bmoff[lv];
     const uint32_t bw = ws.plan.bwd[lv] & ~(1u << dv);
     const uint32_t same = ws.plan.same[lv];
-    uint32_t seg_lo = 0, seg_hi = 0;
-    if ((bw >> lane) & 1u) {
-      const uint32_t* s = g.lseg + uint64_t(f) * W1 + ws.plan.lab[lv];
-      seg_lo = s[0];
-      seg_hi = s[1];
-      bytes += 8;
+    uint32_t seg_lo = c_lo, seg_hi = c_hi;
+    if (c_lv != lv) {  // not the scan right after this depth's enter(): load again
+      if ((bw >> lane) & 1u) {
+        const uint32_t* s = g.lseg + uint64_t(f) * W1 + ws.plan.lab[lv];
+        seg_lo = s[0];
+        seg_hi = s[1];
+        bytes += 8;
+      }
     }
+    c_lv = kInvalid;
     // Leaf ranges of more than two windows: lane j of the same-label depths
     // holds the position of f_j in the driver range (kInvalid when absent); the
     // range has no repeated entry, so f_j can only be the entry at that
@@ -710,9 +728,9 @@ __global__ void __launch_bounds__(kEnumWarps * 32, kEnumMinBlocks) enumerate_ker
   }
   if (cur_q != kInvalid) over_limit();
   flush();
-  bytes = warp_sum(bytes);
+  const unsigned long long all_bytes = warp_sum((unsigned long long)bytes);
   if (lane == 0) {
-    atomicAdd(A.algo_bytes, bytes);
+    atomicAdd(A.algo_bytes, all_bytes);
     atomicAdd(&A.ev[0], (unsigned long long)n_tasks);
     atomicAdd(&A.ev[1], (unsigned long long)n_pops);
     atomicAdd(&A.ev[2], (unsigned long long)n_handoffs);
