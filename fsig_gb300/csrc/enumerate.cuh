@@ -16,11 +16,13 @@
 // segment among the rows of the backward neighbours -- 32 entries at a time,
 // one per lane, filtered by injectivity (against earlier same-label depths),
 // the candidate bitmap of depth i, and membership in every other backward
-// segment.  For membership the warp finds the window of that segment spanned
-// by the 32 driver entries with a 32-ary search (all lanes probe 32 pivots per
-// round, about log32 of the segment length rounds); a window of at most 32
-// entries is then loaded once and searched in registers by shuffles, a longer
-// one by a per-lane binary search inside the window.
+// segment.  Membership is decided by the launch's strategy (kIsect*): by
+// default every surviving lane binary-searches the segment alone; otherwise
+// the warp finds the window of that segment spanned by the 32 driver entries
+// with a 32-ary search (all lanes probe 32 pivots per round, about log32 of
+// the segment length rounds), loads a window of at most 32 entries once and
+// searches it in registers by shuffles, a longer one by a per-lane binary
+// search inside the window.
 //
 // Work stealing: warps that run out of input wait for work.  A busy warp
 // checks every 64 steps whether idle warps outnumber the queued records; if
