@@ -437,11 +437,11 @@ def training_workloads():
     unlabeled 2^20-vertex R-MAT graph is not logged: its 5-vertex patterns
     have about 1e15 embeddings each."""
     from . import workloads as W
-    c5 = W.candidate_specs("c5", rank=40)[0][0][:8192]
+    c5 = W.candidate_specs("c5", rank=40)[0][0]
     dense, sparse = W.candidate_specs("c4", rank=41)[0]
     c4 = [x for pair in zip(dense[:4096], sparse[:4096]) for x in pair]
-    return [("c5", lambda: W.build_graph("c5"), c5, W.WORK_BUDGET, 1024),
-            ("c4", lambda: W.build_graph("c4"), c4, W.WORK_BUDGET, 1024)]
+    return [("c5", lambda: W.build_graph("c5"), c5, W.WORK_BUDGET, 2048),
+            ("c4", lambda: W.build_graph("c4"), c4, W.WORK_BUDGET, 512)]
 
 
 def main(argv=None):
