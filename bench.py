@@ -67,7 +67,7 @@ FALLBACK_HBM_GBS = 6800.0
 # DRAM bytes (read + write) of one enumerate_kernel launch on a config-5
 # batch, from an ncu capture (profiles/enumerate_kernel_c5.md: 648.4 MB/s over
 # 392.1 ms); its loads are served from L2 at about 99 %.
-ENUM_TRAFFIC_BYTES_PER_LAUNCH = 254_200_000
+ENUM_TRAFFIC_BYTES_PER_LAUNCH = 257_250_000
 
 
 def log(*a):

@@ -17,7 +17,8 @@
 // one per lane, filtered by injectivity (against earlier same-label depths),
 // the candidate bitmap of depth i, and membership in every other backward
 // segment.  Membership is decided by the launch's strategy (kIsect*): by
-// default every surviving lane binary-searches the segment alone; otherwise
+// default every surviving lane binary-searches the segments alone, two at a
+// time in lockstep (two independent loads in flight per step); otherwise
 // the warp finds the window of that segment spanned by the 32 driver entries
 // with a 32-ary search (all lanes probe 32 pivots per round, about log32 of
 // the segment length rounds), loads a window of at most 32 entries once and
@@ -91,10 +92,14 @@ struct EnumArgs {
 };
 
 // Membership of a window's entries in a backward segment:
-constexpr uint32_t kIsectBinary = 0;    // every lane binary-searches the rest of the segment alone (default)
+constexpr uint32_t kIsectBinary = 0;    // every lane binary-searches the segments alone, two in lockstep (default)
 constexpr uint32_t kIsectSearch = 1;    // 32-ary window search from the cursor (galloping-like)
 constexpr uint32_t kIsectAdaptive = 2;  // the 32 entries after the cursor first (merge-like), else window search
 constexpr uint32_t kIsectHybrid = 3;    // the tile when the segment's rest fits 32 entries, else as kIsectBinary
+
+// Backward segments searched in lockstep by the default strategy (three
+// spill at 64 registers and run slower).
+constexpr int kGroup = 2;
 
 constexpr uint32_t kErrTimeout = 1u;
 constexpr uint32_t kCtrStride = 32;        // one 128-byte line per counter
@@ -122,6 +127,41 @@ __device__ __forceinline__ bool bsearch_range(const uint32_t* __restrict__ a, ui
     else return true;
   }
   return false;
+}
+
+// Whether x lies in each of the K sorted ranges a[lo[k], hi[k]): the K binary
+// searches run in lockstep, so each step has up to K independent loads in
+// flight; it stops as soon as one search ends without x.
+template <int K>
+__device__ __forceinline__ bool bsearch_all(const uint32_t* __restrict__ a, uint32_t (&lo)[K], uint32_t (&hi)[K],
+                                            uint32_t x, uint32_t& bytes) {
+  bool in[K];
+#pragma unroll
+  for (int k = 0; k < K; k++) in[k] = false;
+  for (;;) {
+    bool s[K], any = false;
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      s[k] = !in[k] && lo[k] < hi[k];
+      if (!in[k] && !s[k]) return false;
+      any |= s[k];
+    }
+    if (!any) return true;
+    uint32_t m[K], y[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      m[k] = (lo[k] + hi[k]) >> 1;
+      y[k] = s[k] ? __ldg(a + m[k]) : 0u;
+      bytes += s[k] ? 4u : 0u;
+    }
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      if (!s[k]) continue;
+      if (y[k] < x) lo[k] = m[k] + 1;
+      else if (y[k] > x) hi[k] = m[k];
+      else in[k] = true;
+    }
+  }
 }
 
 // First index in [lo, hi) of sorted a[] with a[i] >= key (warp-uniform key
@@ -270,6 +310,35 @@ __global__ void __launch_bounds__(kEnumWarps * 32, kEnumMinBlocks) enumerate_ker
   auto member = [&](uint32_t bw, uint32_t x, bool pred, uint32_t& seg_lo, uint32_t seg_hi) -> bool {
     const uint32_t alive = __ballot_sync(kFull, pred);
     if (!bw || !alive) return pred;
+    if (A.isect == kIsectBinary) {
+      // each surviving lane searches alone, kGroup segments at a time
+      while (bw) {
+        uint32_t lo[kGroup], hi[kGroup], k = 0;
+#pragma unroll
+        for (int t = 0; t < kGroup; t++) {
+          lo[t] = hi[t] = 0;
+          if (bw) {
+            const uint32_t j = __ffs(bw) - 1;
+            bw &= bw - 1;
+            lo[t] = __shfl_sync(kFull, seg_lo, j);
+            hi[t] = __shfl_sync(kFull, seg_hi, j);
+            k = t + 1;
+          }
+        }
+        if (pred) {
+          if (k == kGroup) {
+            pred = bsearch_all<kGroup>(g.adj, lo, hi, x, bytes);
+          } else if (kGroup > 2 && k == 2) {
+            uint32_t l2[2] = {lo[0], lo[1]}, h2[2] = {hi[0], hi[1]};
+            pred = bsearch_all<2>(g.adj, l2, h2, x, bytes);
+          } else {
+            pred = bsearch_range(g.adj, lo[0], hi[0], x, bytes);
+          }
+        }
+        if (__ballot_sync(kFull, pred) == 0) break;
+      }
+      return pred;
+    }
     const uint32_t xfirst = __shfl_sync(kFull, x, __ffs(alive) - 1);
     const uint32_t xlast = __shfl_sync(kFull, x, 31 - __clz(alive));
     while (bw) {

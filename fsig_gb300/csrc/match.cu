@@ -589,8 +589,8 @@ void layout_batch(const DeviceGraph& g, const std::vector<HostQuery>& qs, BatchL
       x.u = u;
       x.cls = cls[u];
       x.dom = dom[u];
-      for (uint32_t w = 0; w < h.n; w++)
-        if (cls[w] == cls[u]) x.cmask |= 1u << w;
+      for (uint32_t v = 0; v < h.n; v++)
+        if (cls[v] == cls[u]) x.cmask |= 1u << v;
       std::memcpy(x.sig, h.sig[u], sizeof(x.sig));
       const int32_t l = h.label[u];
       uint32_t lo = 0, hi = 0;

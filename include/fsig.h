@@ -103,12 +103,13 @@ typedef struct {
                                refinement classes (see fsig_refine_classes)      */
   uint32_t isect;           /* set-intersection strategy of the enumeration:
                                0 (default) every lane binary-searches the
-                               segment alone; 1 warp-cooperative 32-ary
-                               window search (galloping-like); 2 adaptive:
-                               the 32 entries after a segment's cursor first
-                               (merge-like), else the window search; 3 the
-                               tile search when the segment's rest fits 32
-                               entries, else as 0                           */
+                               segments alone, two in lockstep; 1 warp-
+                               cooperative 32-ary window search (galloping-
+                               like); 2 adaptive: the 32 entries after a
+                               segment's cursor first (merge-like), else the
+                               window search; 3 the tile search when the
+                               segment's rest fits 32 entries, else a lane's
+                               own binary search                          */
   uint32_t refine_coop;     /* refinement: a candidate's neighbour segment
                                longer than this is scanned by the whole warp
                                (warp per candidate), shorter ones by the
