@@ -31,6 +31,7 @@ OK, EINVAL, ENODEV, ECUDA, EADMISSION, ENOGRAPH, EQUERY, EIO, ETIMEOUT, EOVERFLO
     0, -1, -2, -3, -4, -5, -6, -7, -8, -9, -10)
 ALGO_FSIG, ALGO_GSI, ALGO_FUSED = 1, 2, 3
 ORDER_HEURISTIC, ORDER_LEARNED, ORDER_GIVEN = 0, 1, 2
+SEGMENTS_AUTO, SEGMENTS_TABLE, SEGMENTS_ROWS = 0, 1, 2
 QUERY_INDUCED, QUERY_DENSE, QUERY_SPARSE = 0, 1, 2
 
 
@@ -128,6 +129,8 @@ def engine_library() -> C.CDLL:
     L.fsig_last_stats.argtypes = [vp, C.POINTER(_Stats)]
     L.fsig_filter_noalloc.argtypes = [vp, C.POINTER(_Query), C.c_int, C.c_void_p]
     L.fsig_set_queue_waits.argtypes = [vp, C.c_uint64, C.c_uint64, C.c_int]
+    L.fsig_set_segment_index.argtypes = [vp, C.c_int]
+    L.fsig_graph_layout.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_uint64)]
     L.fsig_match_range.argtypes = [vp, C.POINTER(_Query), C.c_int, C.c_uint32, C.c_uint32, C.c_uint32,
                                    C.POINTER(_Result), C.POINTER(C.c_uint32)]
     fp = C.POINTER(C.c_float)
@@ -151,7 +154,7 @@ def engine_library() -> C.CDLL:
     L.fsig_write_embeddings.argtypes = [vp, C.POINTER(_Query), C.c_int, C.c_char_p, C.POINTER(_Result)]
     for name in ("fsig_mpnn_set_params", "fsig_mpnn_get_params", "fsig_mpnn_features", "fsig_mpnn_forward",
                  "fsig_mpnn_train_step", "fsig_read_graph_file", "fsig_read_graph_file_threads", "fsig_save_graph_cache", "fsig_load_graph_cache", "fsig_graph_file_data", "fsig_match_embeddings",
-                 "fsig_write_embeddings", "fsig_build_pcsr", "fsig_filter_noalloc", "fsig_set_queue_waits", "fsig_match_range", "fsig_last_stats", "fsig_plan_order", "fsig_create", "fsig_destroy", "fsig_load_graph", "fsig_load_graph_file", "fsig_graph_info",
+                 "fsig_write_embeddings", "fsig_build_pcsr", "fsig_filter_noalloc", "fsig_set_queue_waits", "fsig_set_segment_index", "fsig_graph_layout", "fsig_match_range", "fsig_last_stats", "fsig_plan_order", "fsig_create", "fsig_destroy", "fsig_load_graph", "fsig_load_graph_file", "fsig_graph_info",
                  "fsig_match", "fsig_match_batch", "fsig_build_csr", "fsig_build_signature", "fsig_filter",
                  "fsig_filter_classes", "fsig_refine_classes"):
         getattr(L, name).restype = C.c_int
@@ -493,6 +496,19 @@ class Engine:
 
     def load_graph_cache(self, path) -> None:
         self._check(self._L.fsig_load_graph_cache(self._h, str(path).encode()), "load_graph_cache")
+
+    def set_segment_index(self, mode: int = SEGMENTS_AUTO) -> None:
+        """Segment index of the graphs loaded from now on: SEGMENTS_TABLE (a
+        dense V x (L+1) table, one load per lookup), SEGMENTS_ROWS (no table,
+        binary search in the row) or SEGMENTS_AUTO (the table when it takes at
+        most 4 words per adjacency entry).  Results do not depend on it."""
+        self._check(self._L.fsig_set_segment_index(self._h, int(mode)), "set_segment_index")
+
+    def graph_layout(self) -> dict:
+        """The resident store's segment index and its device bytes."""
+        mode, nbytes = C.c_int(), C.c_uint64()
+        self._check(self._L.fsig_graph_layout(self._h, C.byref(mode), C.byref(nbytes)), "graph_layout")
+        return dict(segment_index=mode.value, bytes=nbytes.value)
 
     def graph_info(self) -> dict:
         V, nadj, L, md = C.c_uint32(), C.c_uint64(), C.c_int32(), C.c_uint32()

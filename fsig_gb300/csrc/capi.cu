@@ -132,7 +132,6 @@ int fsig_create(int device, uint64_t arena_bytes, fsig_engine** out) {
   Engine& e = h->e;
   e.device = device;
   e.num_sms = prop.multiProcessorCount;
-  int rc = FSIG_OK;
   auto bail = [&](int code) {
     h->e.last_error = fsig::thread_error();
     if (e.arena.base) cudaFree(e.arena.base);
@@ -160,7 +159,6 @@ int fsig_create(int device, uint64_t arena_bytes, fsig_engine** out) {
   err = cudaMalloc(&e.arena.base, bytes);
   if (err != cudaSuccess) return bail(fsig::fail(FSIG_EADMISSION, "cannot reserve the device arena"));
   e.arena.cap = bytes;
-  (void)rc;
   *out = h;
   return FSIG_OK;
 }
@@ -227,6 +225,22 @@ int fsig_graph_info(const fsig_engine* h, uint32_t* V, uint64_t* nadj, int32_t* 
   if (nadj) *nadj = h->e.g.nadj;
   if (L) *L = h->e.g.L;
   if (maxdeg) *maxdeg = h->e.g.max_deg;
+  return FSIG_OK;
+}
+
+int fsig_set_segment_index(fsig_engine* h, int mode) {
+  if (!h) return FSIG_EINVAL;
+  if (mode != FSIG_SEGMENTS_AUTO && mode != FSIG_SEGMENTS_TABLE && mode != FSIG_SEGMENTS_ROWS)
+    return finish(h, fsig::fail(FSIG_EINVAL, "unknown segment index"));
+  h->e.seg_index = mode;
+  return FSIG_OK;
+}
+
+int fsig_graph_layout(const fsig_engine* h, int* segment_index, uint64_t* bytes) {
+  if (!h) return FSIG_EINVAL;
+  if (!h->e.has_graph) return FSIG_ENOGRAPH;
+  if (segment_index) *segment_index = h->e.g.lseg ? FSIG_SEGMENTS_TABLE : FSIG_SEGMENTS_ROWS;
+  if (bytes) *bytes = fsig::store_bytes(h->e.g);
   return FSIG_OK;
 }
 

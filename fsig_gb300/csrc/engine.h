@@ -17,7 +17,10 @@ constexpr uint32_t kMaxLabels = 4096;  // labels 0..4095 in a loaded data graph
 // space a row of the adjacency sorted by id is also sorted by neighbour
 // label, so the neighbours of v with label l are one contiguous segment
 // [lseg[v*(L+1)+l], lseg[v*(L+1)+l+1]) -- the label-partitioned layout that
-// replaces the reference's hashed PCSR units.
+// replaces the reference's hashed PCSR units.  A store built without the
+// table (FSIG_SEGMENTS_ROWS: V x (L+1) words is large next to the adjacency)
+// finds the same segment by binary search in the row, between the first ids
+// of classes l and l+1 (base).
 struct DeviceGraph {
   uint32_t V = 0;
   int32_t L = 0;
@@ -29,8 +32,8 @@ struct DeviceGraph {
   uint32_t* base = nullptr;        // [L+1] first new id of each label class
   uint32_t* off = nullptr;         // [V+1]
   uint32_t* adj = nullptr;         // [nadj] new ids, rows ascending, no duplicates
-  uint32_t* adj_old = nullptr;     // [nadj] caller id of each adj entry (for the result hash)
-  uint32_t* lseg = nullptr;        // [V*(L+1)]
+  uint32_t* adj_old = nullptr;     // [nadj] caller id of each adj entry (for the result hash); null without lseg
+  uint32_t* lseg = nullptr;        // [V*(L+1)]; null: segments are found by binary search in the rows
   uint4* sig = nullptr;            // [V*4] 64-byte signature per vertex
   std::vector<uint32_t> h_base;    // host copy of base
   uint64_t arena_mark = 0;         // arena top after the graph store
@@ -48,7 +51,9 @@ struct Engine {
   void* pinned = nullptr;
   uint64_t pinned_bytes = 0;
   // enumeration kernel: resident blocks per SM (0 until first queried)
-  int enum_per_sm[9] = {0};  // resident blocks per SM at 1..8 warps per block (0 until queried)
+  int enum_per_sm[9] = {0};       // resident blocks per SM at 1..8 warps per block (0 until queried)
+  int enum_per_sm_rows[9] = {0};  // the same for a graph store without a segment table
+  int seg_index = 0;              // segment index of the next graph build (FSIG_SEGMENTS_*)
   // timing events
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   cudaEvent_t ev_enum[2] = {nullptr, nullptr};
@@ -67,6 +72,8 @@ struct Engine {
 
 // graph_store.cu
 int build_device_graph(Engine& e, uint32_t V, const int32_t* labels, uint64_t E, const uint32_t* edges);
+bool use_segment_table(int mode, uint32_t V, int32_t L, uint64_t nadj);
+uint64_t store_bytes(const DeviceGraph& g);
 int save_graph_cache(Engine& e, const char* path);
 // pcsr.cu
 int build_reference_pcsr(Engine& e, uint32_t V, int32_t L, const int32_t* labels, const uint32_t* off,

@@ -116,6 +116,23 @@ struct WarpSmem {
   uint32_t cand[kMaxQ][kChunk];
 };
 
+// Segment [lo, hi) of row v's neighbours with label l (0 <= l < L): two loads
+// from the dense table, or, in a graph store without one (kRows), two binary
+// searches in the row for the first ids of label classes l and l + 1.
+template <bool kRows>
+__device__ __forceinline__ void row_segment(const GraphView& g, uint32_t v, int32_t l, uint64_t W1, uint32_t& lo,
+                                            uint32_t& hi) {
+  if constexpr (kRows) {
+    const uint32_t b = __ldg(g.off + v), e = __ldg(g.off + v + 1);
+    lo = lower_bound_u32(g.adj, b, e, __ldg(g.base + l));
+    hi = lower_bound_u32(g.adj, lo, e, __ldg(g.base + l + 1));
+  } else {
+    const uint32_t* s = g.lseg + uint64_t(v) * W1 + l;
+    lo = s[0];
+    hi = s[1];
+  }
+}
+
 __device__ __forceinline__ bool bsearch_range(const uint32_t* __restrict__ a, uint32_t lo, uint32_t hi, uint32_t x,
                                               uint32_t& bytes) {
   while (lo < hi) {
@@ -188,6 +205,10 @@ __device__ __forceinline__ uint32_t warp_lower_bound(const uint32_t* __restrict_
   return lo + __popc(__ballot_sync(kFull, in && v < key));
 }
 
+// kRows: the graph store has no segment table (GraphView::lseg is null) and
+// no caller-id copy of the adjacency (adj_old); segments are found in the
+// rows and a leaf's caller id is looked up once it survives.
+template <bool kRows>
 __global__ void __launch_bounds__(kEnumWarps * 32, kEnumMinBlocks) enumerate_kernel(EnumArgs A) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   WarpSmem& ws = reinterpret_cast<WarpSmem*>(smem_raw)[threadIdx.x >> 5];
@@ -271,9 +292,7 @@ __global__ void __launch_bounds__(kEnumWarps * 32, kEnumMinBlocks) enumerate_ker
     const int32_t lab = ws.plan.lab[lv];
     uint32_t lo = 0, hi = 0, len = kInvalid;
     if ((bw >> lane) & 1u) {
-      const uint32_t* s = g.lseg + uint64_t(f) * W1 + lab;
-      lo = s[0];
-      hi = s[1];
+      row_segment<kRows>(g, f, lab, W1, lo, hi);
       len = hi - lo;
       bytes += 8;
     }
@@ -529,9 +548,7 @@ __global__ void __launch_bounds__(kEnumWarps * 32, kEnumMinBlocks) enumerate_ker
     uint32_t seg_lo = c_lo, seg_hi = c_hi;
     if (c_lv != lv) {  // not the scan right after this depth's enter(): load again
       if ((bw >> lane) & 1u) {
-        const uint32_t* s = g.lseg + uint64_t(f) * W1 + ws.plan.lab[lv];
-        seg_lo = s[0];
-        seg_hi = s[1];
+        row_segment<kRows>(g, f, ws.plan.lab[lv], W1, seg_lo, seg_hi);
         bytes += 8;
       }
     }
@@ -564,7 +581,7 @@ __global__ void __launch_bounds__(kEnumWarps * 32, kEnumMinBlocks) enumerate_ker
       const uint32_t k = dp + lane;
       bool pred = lane < nvalid;
       const uint32_t x = pred ? __ldg(g.adj + k) : 0xffffffffu;
-      const uint32_t xo = (pred && leaf) ? __ldg(g.adj_old + k) : 0u;
+      uint32_t xo = (!kRows && pred && leaf) ? __ldg(g.adj_old + k) : 0u;
       if (pred) bytes += leaf ? 8 : 4;
       if (pred) {
         const uint32_t bit = x - bmbase;
@@ -588,6 +605,7 @@ __global__ void __launch_bounds__(kEnumWarps * 32, kEnumMinBlocks) enumerate_ker
         }
       }
       pred = member(bw, x, pred, seg_lo, seg_hi);
+      if (kRows && leaf && pred) xo = __ldg(g.old_of_new + x);
       if (lane == 0) {
         n_examine++;
         if (A.work_cap) pend += nvalid;
@@ -739,8 +757,8 @@ __global__ void __launch_bounds__(kEnumWarps * 32, kEnumMinBlocks) enumerate_ker
           if (ws.plan.n == 1) {
             run(1, kInvalid, kInvalid);
           } else {
-            const uint32_t* s = g.lseg + uint64_t(r) * W1 + ws.plan.lab[1];
-            const uint32_t b0 = s[0], e0 = s[1];
+            uint32_t b0, e0;
+            row_segment<kRows>(g, r, ws.plan.lab[1], W1, b0, e0);
             const uint32_t clo = b0 + c * A.split;
             if (lane == 0) lc += (c == 0);  // the root itself, once
             run(1, clo, min(clo + A.split, e0));

@@ -357,6 +357,19 @@ int build_rows(Engine& e, const uint2* d_edges, uint64_t E, uint32_t V, const ui
 
 }  // namespace
 
+bool use_segment_table(int mode, uint32_t V, int32_t L, uint64_t nadj) {
+  if (mode == FSIG_SEGMENTS_TABLE) return true;
+  if (mode == FSIG_SEGMENTS_ROWS) return false;
+  return uint64_t(V) * (uint64_t(L) + 1) <= 4 * std::max<uint64_t>(nadj, V);
+}
+
+uint64_t store_bytes(const DeviceGraph& g) {
+  const uint64_t V = g.V, L1 = uint64_t(g.L) + 1;
+  uint64_t b = 4 * V * 3 + 4 * L1 + 4 * (V + 1) + 4 * g.nadj + 64 * V;  // label, id maps, base, off, adj, sig
+  if (g.lseg) b += 4 * V * L1 + 4 * g.nadj;                           // lseg, adj_old
+  return b;
+}
+
 int build_device_graph(Engine& e, uint32_t V, const int32_t* h_labels, uint64_t E, const uint32_t* h_edges) {
   cudaStream_t s = e.stream;
   if (V == 0) return fail(FSIG_EINVAL, "graph has no vertices");
@@ -444,20 +457,31 @@ int build_device_graph(Engine& e, uint32_t V, const int32_t* h_labels, uint64_t 
   e.arena.release(mark_tmp);
 
   // Persistent label table, segments and signatures.
+  const bool table = use_segment_table(e.seg_index, V, L, g.nadj);
   g.base = e.arena.take<uint32_t>(uint64_t(L) + 1);
-  g.lseg = e.arena.take<uint32_t>(uint64_t(V) * (uint64_t(L) + 1));
   g.sig = e.arena.take<uint4>(uint64_t(V) * 4);
-  g.adj_old = e.arena.take<uint32_t>(std::max<uint64_t>(g.nadj, 1));
-  if (!g.base || !g.lseg || !g.sig || !g.adj_old) return fail(FSIG_EADMISSION, "graph tables do not fit the device arena");
-  if (g.nadj) {
-    gather_kernel<<<grid_for(g.nadj, 256, e.num_sms), 256, 0, s>>>(g.adj, g.nadj, g.old_of_new, g.adj_old);
-    FSIG_CUDA_TRY(cudaGetLastError());
+  if (table) {
+    g.lseg = e.arena.take<uint32_t>(uint64_t(V) * (uint64_t(L) + 1));
+    g.adj_old = e.arena.take<uint32_t>(std::max<uint64_t>(g.nadj, 1));
   }
+  if (!g.base || !g.sig || (table && (!g.lseg || !g.adj_old)))
+    return fail(FSIG_EADMISSION, "graph tables do not fit the device arena");
   FSIG_CUDA_TRY(cudaMemcpyAsync(g.base, g.h_base.data(), sizeof(uint32_t) * (L + 1), cudaMemcpyHostToDevice, s));
-  label_segments_kernel<<<grid_for(uint64_t(V) * (L + 1), 256, e.num_sms), 256, 0, s>>>(g.off, g.adj, g.base, V, L,
-                                                                                       g.lseg);
-  FSIG_CUDA_TRY(cudaGetLastError());
-  signature_from_segments_kernel<<<grid_for(V, 128, e.num_sms), 128, 0, s>>>(g.label, g.lseg, V, L, g.sig);
+  if (table) {
+    if (g.nadj) {
+      gather_kernel<<<grid_for(g.nadj, 256, e.num_sms), 256, 0, s>>>(g.adj, g.nadj, g.old_of_new, g.adj_old);
+      FSIG_CUDA_TRY(cudaGetLastError());
+    }
+    label_segments_kernel<<<grid_for(uint64_t(V) * (L + 1), 256, e.num_sms), 256, 0, s>>>(g.off, g.adj, g.base, V,
+                                                                                         L, g.lseg);
+    FSIG_CUDA_TRY(cudaGetLastError());
+    signature_from_segments_kernel<<<grid_for(V, 128, e.num_sms), 128, 0, s>>>(g.label, g.lseg, V, L, g.sig);
+  } else {
+    // one saturating increment per neighbour (rows have no duplicates) gives
+    // every label segment's min(count, 2) increments
+    signature_from_rows_kernel<<<grid_for(V, 128, e.num_sms), 128, 0, s>>>(g.label, g.off, g.adj, V, 0,
+                                                                           reinterpret_cast<uint32_t*>(g.sig));
+  }
   FSIG_CUDA_TRY(cudaGetLastError());
   // Maximum degree.
   uint32_t* mx = e.arena.take<uint32_t>(1);
@@ -490,13 +514,15 @@ int build_device_graph(Engine& e, uint32_t V, const int32_t* h_labels, uint64_t 
 namespace {
 constexpr char kCacheMagic[8] = {'F', 'S', 'I', 'G', 'G', 'S', '0', '1'};
 
+constexpr uint32_t kCacheRows = 1u;  // CacheHeader::flags: a store without lseg and adj_old
+
 struct CacheHeader {
   char magic[8];
   uint32_t V;
   int32_t L;
   uint64_t nadj;
   uint32_t max_deg;
-  uint32_t pad;
+  uint32_t flags;
 };
 
 struct CacheArray {
@@ -504,11 +530,17 @@ struct CacheArray {
   uint64_t bytes;
 };
 
-std::vector<CacheArray> cache_arrays(const DeviceGraph& g) {
+std::vector<CacheArray> cache_arrays(const DeviceGraph& g, bool table) {
   const uint64_t V = g.V, L1 = uint64_t(g.L) + 1;
-  return {{g.label, 4 * V},           {g.old_of_new, 4 * V},     {g.new_of_old, 4 * V},
-          {g.base, 4 * L1},           {g.off, 4 * (V + 1)},      {g.adj, 4 * g.nadj},
-          {g.adj_old, 4 * g.nadj},    {g.lseg, 4 * V * L1},      {g.sig, 64 * V}};
+  return {{g.label, 4 * V},
+          {g.old_of_new, 4 * V},
+          {g.new_of_old, 4 * V},
+          {g.base, 4 * L1},
+          {g.off, 4 * (V + 1)},
+          {g.adj, 4 * g.nadj},
+          {g.adj_old, table ? 4 * g.nadj : 0},
+          {g.lseg, table ? 4 * V * L1 : 0},
+          {g.sig, 64 * V}};
 }
 }  // namespace
 
@@ -523,9 +555,10 @@ int save_graph_cache(Engine& e, const char* path) {
   h.L = g.L;
   h.nadj = g.nadj;
   h.max_deg = g.max_deg;
+  h.flags = g.lseg ? 0u : kCacheRows;
   bool ok = std::fwrite(&h, sizeof h, 1, f) == 1;
   std::vector<char> buf;
-  for (const CacheArray& a : cache_arrays(g)) {
+  for (const CacheArray& a : cache_arrays(g, g.lseg != nullptr)) {
     if (!ok) break;
     buf.resize(a.bytes);
     if (a.bytes) {
@@ -545,7 +578,8 @@ int load_graph_cache(Engine& e, const char* path) {
   FILE* f = std::fopen(path, "rb");
   if (!f) return fail(FSIG_EIO, std::string("cannot open ") + path);
   CacheHeader h{};
-  if (std::fread(&h, sizeof h, 1, f) != 1 || std::memcmp(h.magic, kCacheMagic, 8) != 0 || h.V == 0 || h.L < 1) {
+  if (std::fread(&h, sizeof h, 1, f) != 1 || std::memcmp(h.magic, kCacheMagic, 8) != 0 || h.V == 0 || h.L < 1 ||
+      h.L > int32_t(kMaxLabels) || (h.flags & ~kCacheRows) != 0) {
     std::fclose(f);
     return fail(FSIG_EIO, std::string(path) + " is not a graph cache of this engine");
   }
@@ -562,17 +596,21 @@ int load_graph_cache(Engine& e, const char* path) {
   g.new_of_old = e.arena.take<uint32_t>(V);
   g.off = e.arena.take<uint32_t>(V + 1);
   g.adj = e.arena.take<uint32_t>(std::max<uint64_t>(g.nadj, 1));
+  const bool table = (h.flags & kCacheRows) == 0;
   g.base = e.arena.take<uint32_t>(L1);
-  g.lseg = e.arena.take<uint32_t>(V * L1);
   g.sig = e.arena.take<uint4>(V * 4);
-  g.adj_old = e.arena.take<uint32_t>(std::max<uint64_t>(g.nadj, 1));
-  if (!g.label || !g.old_of_new || !g.new_of_old || !g.off || !g.adj || !g.base || !g.lseg || !g.sig || !g.adj_old) {
+  if (table) {
+    g.lseg = e.arena.take<uint32_t>(V * L1);
+    g.adj_old = e.arena.take<uint32_t>(std::max<uint64_t>(g.nadj, 1));
+  }
+  if (!g.label || !g.old_of_new || !g.new_of_old || !g.off || !g.adj || !g.base || !g.sig ||
+      (table && (!g.lseg || !g.adj_old))) {
     std::fclose(f);
     e.arena.release(0);
     return fail(FSIG_EADMISSION, "graph does not fit the device arena");
   }
   std::vector<char> buf;
-  for (const CacheArray& a : cache_arrays(g)) {
+  for (const CacheArray& a : cache_arrays(g, table)) {
     buf.resize(a.bytes);
     if (a.bytes && std::fread(buf.data(), 1, a.bytes, f) != a.bytes) {
       std::fclose(f);

@@ -30,7 +30,8 @@ struct GraphView {
   const uint32_t* __restrict__ lseg;
   const uint4* __restrict__ sig;
   const uint32_t* __restrict__ old_of_new;
-  const uint32_t* __restrict__ adj_old;
+  const uint32_t* __restrict__ adj_old;  // null when lseg is
+  const uint32_t* __restrict__ base;     // [L+1] first id of each label class
 };
 
 namespace {
@@ -39,7 +40,21 @@ constexpr uint32_t kFull = 0xffffffffu;
 constexpr int kChunk = 32;  // driver elements examined per refill (one per lane)
 
 GraphView view_of(const DeviceGraph& g) {
-  return GraphView{g.V, g.L, g.label, g.off, g.adj, g.lseg, g.sig, g.old_of_new, g.adj_old};
+  return GraphView{g.V, g.L, g.label, g.off, g.adj, g.lseg, g.sig, g.old_of_new, g.adj_old, g.base};
+}
+
+// Segment [lo, hi) of row v's neighbours with label l (0 <= l < L), from the
+// dense table when the store has one, else by two binary searches in the row.
+__device__ __forceinline__ void segment_of(const GraphView& g, uint32_t v, int32_t l, uint32_t& lo, uint32_t& hi) {
+  if (g.lseg) {
+    const uint32_t* s = g.lseg + uint64_t(v) * (uint64_t(g.L) + 1) + l;
+    lo = s[0];
+    hi = s[1];
+  } else {
+    const uint32_t b = __ldg(g.off + v), e = __ldg(g.off + v + 1);
+    lo = lower_bound_u32(g.adj, b, e, __ldg(g.base + l));
+    hi = lower_bound_u32(g.adj, lo, e, __ldg(g.base + l + 1));
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -185,7 +200,6 @@ __global__ void __launch_bounds__(256) refine_kernel(GraphView g, const QVert* _
                                                      uint32_t coop_min) {
   const uint32_t lane = threadIdx.x & 31;
   const uint64_t nwt = (uint64_t(gridDim.x) * blockDim.x) >> 5;
-  const uint64_t W1 = uint64_t(g.L) + 1;
   for (uint64_t run = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; run * kRefineRun < total_words;
        run += nwt) {
     uint64_t W = run * kRefineRun;
@@ -227,11 +241,7 @@ __global__ void __launch_bounds__(256) refine_kernel(GraphView g, const QVert* _
         const uint32_t* __restrict__ nb = src + qw->bmoff;
         const uint32_t nbase = qw->bmbase;
         uint32_t k = 0, e = 0;
-        if (alive) {
-          const uint32_t* s = g.lseg + uint64_t(v) * W1 + qw->label;
-          k = s[0];
-          e = s[1];
-        }
+        if (alive) segment_of(g, v, qw->label, k, e);
         const bool coop = alive && e - k > coop_min;
         if (alive && !coop) {
           uint32_t have = 0;
@@ -449,14 +459,13 @@ __global__ void root_chunks_kernel(GraphView g, const Plan* __restrict__ plans, 
                                    const uint32_t* __restrict__ root_q, const uint32_t* __restrict__ total_roots,
                                    uint32_t split, uint32_t* chunks) {
   const uint32_t nr = *total_roots;
-  const uint64_t W1 = uint64_t(g.L) + 1;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nr; i += gridDim.x * blockDim.x) {
     const Plan* p = plans + root_q[i];
     uint32_t c = 1;
     if (p->n > 1) {
-      const uint32_t* s = g.lseg + uint64_t(roots[i]) * W1 + p->lab[1];
-      const uint32_t len = s[1] - s[0];
-      c = max(1u, (len + split - 1) / split);
+      uint32_t lo, hi;
+      segment_of(g, roots[i], p->lab[1], lo, hi);
+      c = max(1u, (hi - lo + split - 1) / split);
     }
     chunks[i] = c;
   }
@@ -749,17 +758,25 @@ struct EnumRun {
 };
 
 // One-time kernel attributes and occupancy (host calls, kept out of captures).
-int enum_configure(Engine& e) {
-  if (e.enum_per_sm[kEnumWarps]) return FSIG_OK;
-  FSIG_CUDA_TRY(cudaFuncSetAttribute(enumerate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+template <bool kRows>
+int enum_configure_one(int* per_sm) {
+  FSIG_CUDA_TRY(cudaFuncSetAttribute(enumerate_kernel<kRows>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      int(sizeof(WarpSmem) * kEnumWarps)));
   for (uint32_t w = 1; w <= kEnumWarps; w++) {
     int per = 0;
-    FSIG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, enumerate_kernel, int(w * 32),
+    FSIG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, enumerate_kernel<kRows>, int(w * 32),
                                                                 sizeof(WarpSmem) * w));
-    e.enum_per_sm[w] = std::max(per, 1);
+    per_sm[w] = std::max(per, 1);
   }
   return FSIG_OK;
+}
+
+int enum_configure(Engine& e) {
+  if (e.enum_per_sm[kEnumWarps]) return FSIG_OK;
+  int rc = enum_configure_one<false>(e.enum_per_sm);
+  if (!rc) rc = enum_configure_one<true>(e.enum_per_sm_rows);
+  if (rc) e.enum_per_sm[kEnumWarps] = 0;
+  return rc;
 }
 
 int enum_prepare(Engine& e, const BatchOptions& opt, const GraphView& gv, const Plan* d_plans, const uint32_t* pool,
@@ -780,7 +797,7 @@ int enum_prepare(Engine& e, const BatchOptions& opt, const GraphView& gv, const 
   FSIG_CUDA_TRY(cudaMemsetAsync(R.d_ev, 0, 64, s));
   FSIG_CUDA_TRY(cudaMemsetAsync(d_misc + 1, 0, sizeof(unsigned long long), s));
   const uint32_t wpb = std::max<uint32_t>(1, std::min<uint32_t>(opt.warps_per_block, kEnumWarps));
-  const int per_sm = e.enum_per_sm[wpb];
+  const int per_sm = gv.lseg ? e.enum_per_sm[wpb] : e.enum_per_sm_rows[wpb];
   R.smem = sizeof(WarpSmem) * wpb;
   R.grid = uint32_t(e.num_sms * per_sm);
   R.block = wpb * 32;
@@ -832,7 +849,8 @@ int enum_launch(Engine& e, EnumRun& R) {
   ctr_init_kernel<<<1, 256, 0, s>>>(R.ctr, R.pass == 0 ? R.first_task : 0u, R.active);
   FSIG_CUDA_TRY(cudaGetLastError());
   FSIG_CUDA_TRY(record(e.ev_enum[0], s));
-  enumerate_kernel<<<R.grid, R.block, R.smem, s>>>(R.A);
+  if (R.A.g.lseg) enumerate_kernel<false><<<R.grid, R.block, R.smem, s>>>(R.A);
+  else enumerate_kernel<true><<<R.grid, R.block, R.smem, s>>>(R.A);
   FSIG_CUDA_TRY(cudaGetLastError());
   FSIG_CUDA_TRY(record(e.ev_enum[1], s));
   FSIG_CUDA_TRY(cudaMemcpyAsync(R.h_ctr, R.ctr, sizeof(uint32_t) * 4 * kCtrStride, cudaMemcpyDeviceToHost, s));

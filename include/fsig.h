@@ -52,6 +52,13 @@ extern "C" {
 #define FSIG_ALGO_GSI 2   /* label+signature filter, candidate-count order with 0.9 decay (GSI)                  */
 #define FSIG_ALGO_FUSED 3 /* all filters + refinement, candidate-count order                                      */
 
+/* segment index of the resident graph store (fsig_set_segment_index) */
+#define FSIG_SEGMENTS_AUTO 0  /* TABLE when it takes at most 4 words per adjacency entry, else ROWS */
+#define FSIG_SEGMENTS_TABLE 1 /* dense table of every row's label-segment starts, V x (L+1) words,
+                                 plus the caller id of every adjacency entry: one load per lookup  */
+#define FSIG_SEGMENTS_ROWS 2  /* no table: a segment is found by binary search in its row, a
+                                 leaf's caller id by one lookup once it survives                    */
+
 /* order sources */
 #define FSIG_ORDER_HEURISTIC 0 /* the algorithm's own order                         */
 #define FSIG_ORDER_LEARNED 1   /* the loaded order-scoring network (fsig_mpnn_*)    */
@@ -141,6 +148,17 @@ int fsig_load_graph(fsig_engine* e, uint32_t num_vertices, const int32_t* labels
 int fsig_load_graph_file(fsig_engine* e, const char* path, int is_labeled);
 int fsig_graph_info(const fsig_engine* e, uint32_t* num_vertices, uint64_t* num_adj,
                     int32_t* num_labels, uint32_t* max_degree);
+/* Segment index (FSIG_SEGMENTS_*) of the graphs the engine builds from now on
+ * (fsig_load_graph, fsig_load_graph_file; a cache keeps the index it was
+ * saved with).  Results do not depend on it.  The dense table costs
+ * 4 V (L+1) + 4 x adjacency bytes; without it a graph of many labels fits in
+ * about half the memory of its adjacency and signatures, and lookups cost
+ * two binary searches in a row.  Replaces nothing in the reference, whose
+ * PCSR units are sized per label pair (graph_format_transformer.cc:39-215). */
+int fsig_set_segment_index(fsig_engine* e, int mode);
+/* The resident store's index (FSIG_SEGMENTS_TABLE or _ROWS) and its device
+ * bytes (every array kept for matching). */
+int fsig_graph_layout(const fsig_engine* e, int* segment_index, uint64_t* store_bytes);
 
 /* Binary cache of the resident graph store (the device arrays as built: the
  * renumbered CSR, caller ids, label segments and signatures), in place of the
