@@ -8,7 +8,6 @@ import socket
 import sys
 from pathlib import Path
 
-import numpy as np
 import pytest
 import torch.multiprocessing as mp
 

@@ -6,7 +6,6 @@ the reference's MMatch::find_equivalent_classes (match/MMatch.cu:44-173,
 recorded in the golden fixtures), the dominated classes, and the oracle's
 refinement rule: stronger than the per-vertex rule and never dropping the
 image of an embedding (brute force on small graphs)."""
-import itertools
 
 import numpy as np
 import pytest
