@@ -197,12 +197,13 @@ def cuda_sync():
 # ---------------------------------------------------------------------------
 # the CPU oracle on a fixed subset of a batch (cpu_baseline, reference arm)
 # ---------------------------------------------------------------------------
-def oracle_on(w: W.Workload, queries) -> tuple:
+def oracle_on(w: W.Workload, queries, threads: int = 0) -> tuple:
     """(results [(count, hash)], seconds, threads): the oracle's backtracking
-    matcher on the host cores, every query to completion."""
+    matcher on the host cores (all of them unless threads is given), every
+    query to completion."""
     from oracle import oracle as O  # the CPU legs only
     off, adj = w.csr
-    threads = os.cpu_count() or 1
+    threads = threads or os.cpu_count() or 1
     t0 = time.perf_counter()
     res = []
     for q in queries:
@@ -426,6 +427,12 @@ def run_ours(args, dist):
                                 "embeddings_per_s": sig(cemb / cdt),
                                 "sample": f"batch 0's reference subset: {len(qs)} queries ({cemb} embeddings), "
                                           f"oracle backtracking, {threads} threads, {cdt:.1f}s"}
+        # the same oracle on one thread, over the subset's first query
+        o1, t1, _ = oracle_on(w, qs[:1], threads=1)
+        t1 = max(t1, 1e-9)
+        line["cpu_baseline"]["single_thread"] = {
+            "value": sig(1 / t1), "unit": "queries/s", "embeddings_per_s": sig(o1[0][0] / t1),
+            "sample": f"the subset's first query ({o1[0][0]} embeddings), 1 thread, {t1:.1f}s"}
         line["oracle_check"] = {"queries": len(qs), "equal": bool(equal),
                                 "note": "oracle (count, hash) against the timed step-0 results of the same queries"}
         line["matched_subset"]["cpu_qps_batch0"] = sig(len(qs) / cdt)
