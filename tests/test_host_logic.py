@@ -180,3 +180,13 @@ def test_batch_packing_matches_per_query_packing():
         assert bool(a.order) == (q.order is not None)
         if q.order is not None:
             assert list(a.order[:a.num_vertices]) == q.order.tolist()
+
+
+def test_batch_packing_refuses_an_order_of_the_wrong_length():
+    """Each order pointer is placed by its query's vertex count, so an order
+    of another length would shift every later query's: refused up front."""
+    q = F.Query(np.zeros(3, np.int32), np.array([[0, 1], [1, 2]], np.uint32))
+    bad = F.Query(q.labels, q.edges, order=np.arange(2, dtype=np.uint32))
+    with pytest.raises(ValueError):
+        F._pack_queries([q, bad, q])
+    F._pack_queries([q, F.Query(q.labels, q.edges, order=np.arange(3, dtype=np.uint32))])
