@@ -600,4 +600,88 @@ int orc_match(uint32_t V, const int32_t* labels, const uint32_t* off, const uint
   return 0;
 }
 
+// K4 subgraphs of a simple graph, listed once each: every edge oriented
+// towards the endpoint of higher (degree, id) rank, then for every oriented
+// edge (u, v) the common out-neighbours W of u and v, and for every w in W
+// its out-neighbours in W.  Also returns the number of embeddings of K4 plus
+// a pendant vertex at query vertex 0 (the K4+pendant identity): each K4
+// subgraph has 24 embeddings, each of its vertices the image of vertex 0 in
+// 6 of them, and the pendant is any neighbour of that image outside the
+// other three, so the count is 6 * sum over K4 subgraphs of the sum of
+// (deg - 3) over their vertices.  A cross-check for counting at scales the
+// backtracking matcher cannot finish; returns 0, negative on bad input.
+int orc_k4_pendant(uint32_t V, const uint32_t* off, const uint32_t* adj, int num_threads, uint64_t* k4,
+                   uint64_t* pendant) {
+  if (!off || !k4 || !pendant || (off[V] && !adj)) return -1;
+  auto before = [&](uint32_t a, uint32_t b) {
+    const uint32_t da = off[a + 1] - off[a], db = off[b + 1] - off[b];
+    return da < db || (da == db && a < b);
+  };
+  std::vector<uint64_t> oo(size_t(V) + 1, 0);
+  for (uint32_t v = 0; v < V; v++) {
+    uint64_t c = 0;
+    for (uint32_t i = off[v]; i < off[v + 1]; i++) c += before(v, adj[i]) ? 1 : 0;
+    oo[v + 1] = oo[v] + c;
+  }
+  std::vector<uint32_t> oe(oo[V]);
+  for (uint32_t v = 0; v < V; v++) {
+    uint64_t k = oo[v];
+    for (uint32_t i = off[v]; i < off[v + 1]; i++)
+      if (before(v, adj[i])) oe[k++] = adj[i];
+  }
+  if (num_threads <= 0) num_threads = int(std::max(1u, std::thread::hardware_concurrency()));
+  std::atomic<uint32_t> next{0};
+  std::vector<uint64_t> cnt(size_t(num_threads), 0), wsum(size_t(num_threads), 0);
+  auto worker = [&](int t) {
+    std::vector<uint32_t> m1(V, 0), m2(V, 0), W;
+    uint32_t stamp2 = 0;
+    uint64_t c = 0, s = 0;
+    for (;;) {
+      const uint32_t u0 = next.fetch_add(64);
+      if (u0 >= V) break;
+      for (uint32_t u = u0; u < std::min(V, u0 + 64); u++) {
+        for (uint64_t i = oo[u]; i < oo[u + 1]; i++) m1[oe[i]] = u + 1;
+        const uint64_t du = off[u + 1] - off[u];
+        for (uint64_t i = oo[u]; i < oo[u + 1]; i++) {
+          const uint32_t v = oe[i];
+          W.clear();
+          for (uint64_t j = oo[v]; j < oo[v + 1]; j++)
+            if (m1[oe[j]] == u + 1) W.push_back(oe[j]);
+          if (W.size() < 2) continue;
+          if (++stamp2 == 0) {  // wrapped: clear and restart the stamps
+            std::fill(m2.begin(), m2.end(), 0u);
+            stamp2 = 1;
+          }
+          for (uint32_t w : W) m2[w] = stamp2;
+          const uint64_t duv = du + (off[v + 1] - off[v]);
+          for (uint32_t w : W) {
+            const uint64_t duvw = duv + (off[w + 1] - off[w]);
+            for (uint64_t j = oo[w]; j < oo[w + 1]; j++) {
+              const uint32_t x = oe[j];
+              if (m2[x] == stamp2) {
+                c++;
+                s += duvw + (off[x + 1] - off[x]) - 12;
+              }
+            }
+          }
+        }
+      }
+    }
+    cnt[size_t(t)] = c;
+    wsum[size_t(t)] = s;
+  };
+  std::vector<std::thread> th;
+  for (int t = 1; t < num_threads; t++) th.emplace_back(worker, t);
+  worker(0);
+  for (auto& t : th) t.join();
+  uint64_t C = 0, S = 0;
+  for (int t = 0; t < num_threads; t++) {
+    C += cnt[size_t(t)];
+    S += wsum[size_t(t)];
+  }
+  *k4 = C;
+  *pendant = 6 * S;
+  return 0;
+}
+
 }  // extern "C"

@@ -82,6 +82,12 @@ int orc_match(uint32_t V, const int32_t* labels, const uint32_t* offsets, const 
               const uint32_t* order, int num_threads, uint64_t hash_seed,
               uint64_t* count, uint64_t* hash, uint64_t* level_counts);
 
+// K4 subgraphs of a simple graph (symmetric CSR, no duplicates or
+// self-loops) and the number of embeddings of K4 plus a pendant at query
+// vertex 0, by the identity 6 * sum over K4s of sum of (deg - 3).
+int orc_k4_pendant(uint32_t V, const uint32_t* offsets, const uint32_t* edges, int num_threads, uint64_t* k4,
+                   uint64_t* pendant);
+
 #ifdef __cplusplus
 }
 #endif

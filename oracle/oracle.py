@@ -55,6 +55,8 @@ def _load():
     L.orc_match.restype = C.c_int
     L.orc_match.argtypes = [C.c_uint32, i32p, u32p, u32p, C.c_uint32, i32p, C.c_uint32, u32p, C.c_void_p, C.c_int,
                             C.c_uint64, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), u64p]
+    L.orc_k4_pendant.restype = C.c_int
+    L.orc_k4_pendant.argtypes = [C.c_uint32, u32p, u32p, C.c_int, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
     _lib = L
     return L
 
@@ -225,6 +227,21 @@ def match(labels, offsets, edges, qlabels, qedges, order=None, threads=0, seed=N
     if rc != 0:
         raise ValueError(f"oracle rejected the query (code {rc})")
     return cnt.value, hsh.value, lv[:n].copy()
+
+
+def k4_pendant(offsets, edges, threads=0):
+    """(K4 subgraphs, embeddings of K4 plus a pendant) of a simple graph, by
+    clique listing and the identity 6 * sum over K4s of sum of (deg - 3)."""
+    L = _load()
+    off = np.ascontiguousarray(offsets, np.uint32)
+    e = np.ascontiguousarray(edges, np.uint32)
+    if e.size == 0:
+        e = np.zeros(1, np.uint32)
+    k4, pend = C.c_uint64(), C.c_uint64()
+    rc = L.orc_k4_pendant(len(off) - 1, off, e, int(threads), C.byref(k4), C.byref(pend))
+    if rc != 0:
+        raise ValueError(f"oracle rejected the graph (code {rc})")
+    return k4.value, pend.value
 
 
 def ref_dump(*args) -> str:
