@@ -5,8 +5,10 @@ checks every pattern there), no labels, and the five 5-vertex patterns -- K4 plu
 two seeded random connected graphs.  Skewed degree lists stress the segment
 searches.  Pins: the K4+pendant identity (its count is the sum over ordered
 K4 embeddings of deg(image of the attach vertex) - 3, with the K4 embeddings
-taken from the embedding output), agreement of the three algorithms and of the
-batched path, and the oracle where it finishes quickly."""
+taken from the embedding output; and at 2^12 vertices and 2^16 edges, the
+config-3 density, from the oracle's clique listing), agreement of the three
+algorithms and of the batched path, and the oracle where it finishes
+quickly."""
 import numpy as np
 import pytest
 
@@ -71,6 +73,22 @@ def test_k4_pendant_identity(engine, rmat):
     expect = int((deg[rows[:, 0]] - 3).sum())
     r = engine.match(pattern(PATTERNS["k4_pendant"]), F.ALGO_FSIG)
     assert r.count == expect
+
+
+def test_k4_pendant_identity_at_config3_density(engine):
+    """R-MAT 2^12 / 2^16 (16 edges per vertex, as in config 3): the engine's
+    K4 count (2.4e8 embeddings) and K4+pendant count (1.0e11) against the
+    oracle's clique listing and the identity 6 * sum over K4s of the sum of
+    (deg - 3) -- a pin at a scale the backtracking oracle does not reach."""
+    g = F.gen_rmat(1 << 12, 1 << 16, 0.57, 0.19, 0.19, seed=3)
+    off, adj = g.csr()
+    k4, pend = O.k4_pendant(off, adj)
+    engine.load_graph(g)
+    q4 = F.Query(np.zeros(4, np.int32), np.asarray(PATTERNS["k4_pendant"][:6], np.uint32))
+    r4 = engine.match(q4, F.ALGO_GSI)
+    assert (r4.status, r4.count) == (0, 24 * k4)
+    r = engine.match(pattern(PATTERNS["k4_pendant"]), F.ALGO_GSI)
+    assert (r.status, r.count) == (0, pend)
 
 
 @pytest.mark.parametrize("name", sorted(PATTERNS))
